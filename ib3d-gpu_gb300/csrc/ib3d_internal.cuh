@@ -1,0 +1,195 @@
+// Internal declarations shared by the IB3D CUDA translation units.
+//
+// Device layout (one context = one grid on one GPU, everything resident in HBM):
+//   * 3-D FP64 fields u,v,w,ut,vt,wt,p,pc,b,bdt in the reference's Fortran layout
+//     (nx+2, ny+2, nz+2), i fastest, so that upload/download are plain copies.
+//   * cell flags as uint8 (0 fluid, 1 solid, 2 immersed-boundary) in the same layout,
+//     and an int32 map from a cell to its immersed-boundary index (-1 elsewhere).
+//   * 1-D grid tables (coordinates, spacings, Poisson and convection coefficients,
+//     plus 1-D quotients the kernels would otherwise recompute per cell).
+//   * FP32 scratch e32/r32 for the mixed-precision pressure solve.
+//   * per-immersed-boundary-cell geometry and the ghost-point schedule.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ib3d.h"
+
+namespace ib3d {
+
+constexpr int kBlock = 256;
+
+// Index helpers: 1-based Fortran (i,j,k) into the padded column-major array.
+struct Dims {
+  int nx, ny, nz;      // interior cells
+  int NX2, NY2, NZ2;   // padded extents
+  long long n3;        // padded cell count
+  __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+    return (long long)(i - 1) + (long long)NX2 * ((long long)(j - 1) + (long long)NY2 * (long long)(k - 1));
+  }
+};
+
+// 1-D device tables; every pointer is 1-based (element 0 unused) unless noted.
+struct Grid1D {
+  const double *x1, *y1, *z1, *dx, *dy, *dz;
+  const double *xu, *yu, *zu, *xv, *yv, *zv, *xw, *yw, *zw, *xp, *yp, *zp;
+  // Poisson coefficients, 1-based by interior index (Acx(i-1,c) of the reference
+  // is acx[c][i-1]); [0..2] = columns 1..3.
+  const double *acx[3], *acy[3], *acz[3];
+  const float *acx32[3], *acy32[3], *acz32[3];
+  // convection tables cc[fam][m], fam 0 uu,1 vv,2 ww,3 uv(=uw),4 vu(=vw),5 wu(=wv)
+  const double* cc[6][12];
+  // velocity-correction factor deltat/(0.5*(d(i+1)+d(i))) per axis
+  const double *corx, *cory, *corz;
+};
+
+// Shared control block of the sweep loop; lives in device memory.
+struct SolveCtl {
+  unsigned long long upd;     // max |delta pc| of the running sweep (bit pattern, >= 0)
+  unsigned long long res;     // max |residual| of the running check (bit pattern)
+  unsigned long long aux;     // divmax / derrStdSt accumulator (bit pattern)
+  unsigned int tickets;       // finished-block counter of the deciding kernel
+  int done;                   // 0 running, 1 converged, 2 sweep cap reached
+  long long nsweeps;          // sweep at which the loop stopped
+  double final_err;           // stopping-test value at that sweep
+  double last_res;            // last residual measured
+};
+
+// Per-op data of the ghost-point schedule. An op is one ghost value: six per
+// immersed-boundary cell for the velocity (blocks U2,U1,V2,V1,W2,W1 in
+// subForcing.f90's order) and one for the pressure.
+struct ForceSched {
+  int nops;
+  int nlevels;
+  int* order;        // op ids sorted by level (device)
+  std::vector<int> level_off;  // host: start of each level in `order`, size nlevels+1
+  int* rd_idx;       // 8 linear read indices per op (device)
+  int* rd_src;       // 8 sources per op: op id that wrote it earlier, or -1 (device)
+  int* tgt;          // linear target index per op (device)
+  int* brk;          // 3 bracket indices per op (device)
+  unsigned char* fin;// 1 if the op is the last writer of its target (device)
+  double* out;       // ghost value per op (device)
+  int* final_ops;    // ops with fin = 1 (device)
+  int nfinal;
+};
+
+}  // namespace ib3d
+
+struct ib3d_ctx {
+  ib3d::Dims d;
+  ib3d_params prm;
+  cudaStream_t st = nullptr;
+  int device = 0;
+  std::string err;
+
+  // host copies of the 1-D tables (1-based std::vectors)
+  std::vector<double> hx1, hy1, hz1, hdx, hdy, hdz;
+  std::vector<double> hxu, hyu, hzu, hxv, hyv, hzv, hxw, hyw, hzw, hxp, hyp, hzp;
+  std::vector<double> hac[3][3];
+  std::vector<double> hcc[6][12];
+
+  // device storage
+  double* d_tables = nullptr;  // all 1-D FP64 tables in one allocation
+  float* d_tables32 = nullptr;
+  ib3d::Grid1D g{};
+  double *u = nullptr, *v = nullptr, *w = nullptr, *ut = nullptr, *vt = nullptr, *wt = nullptr;
+  double *p = nullptr, *pc = nullptr, *b = nullptr, *bdt = nullptr;
+  float *e32 = nullptr, *r32 = nullptr;
+  unsigned char* cell = nullptr;
+  int* ibmap = nullptr;
+  ib3d::SolveCtl* ctl = nullptr;
+  ib3d::SolveCtl* h_ctl = nullptr;  // pinned mirror
+
+  // surface mesh
+  long long nnodes = 0, nelems = 0, inor = 1;
+  double* d_nodes = nullptr;  // 3*nnodes shifted node coordinates (x block, y block, z block)
+  int* d_tri = nullptr;       // 3*nelems 1-based node ids
+  double* d_surf = nullptr;   // 9*nelems: xc,yc,zc,cosA,cosB,cosG,alpha3,beta3,gamma3
+
+  // search results
+  bool searched = false;
+  long long counts[5] = {0, 0, 0, 0, 0};
+  int nib = 0;
+  int* d_iblist = nullptr;    // 3*nib (i block, j block, k block), 1-based
+  int* d_nelp = nullptr;      // nib, 1-based element ids
+  double* d_nd = nullptr;     // 7*nib normal distances (p,u1,u2,v1,v2,w1,w2)
+  int* d_minel = nullptr;     // box-sized nearest element
+  long long box[6] = {0, 0, 0, 0, 0, 0};
+
+  ib3d::ForceSched fv{};  // velocity ghost points
+  ib3d::ForceSched fp{};  // pressure ghost points
+
+  // drag/lift
+  bool have_scache = false;
+  int* d_scache = nullptr;     // 15*nelems: cell, u, v, w, p brackets (3 each)
+  double* d_contrib = nullptr; // 7*nelems per-element terms
+  double* d_coef = nullptr;    // 4 coefficients
+  int* d_flag = nullptr;       // device error flag (probe out of grid)
+
+  // reduction / scan scratch
+  long long* d_scan = nullptr;
+  size_t scan_cap = 0;
+};
+
+// ---- kernel launchers (defined in the .cu files) ----
+namespace ib3d {
+// k_pressure.cu
+void launch_divergence(ib3d_ctx* c, bool zero_pc);
+int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st);
+int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st);
+void launch_correct(ib3d_ctx* c);
+void launch_velocity_bc(ib3d_ctx* c);
+void launch_solid_bc(ib3d_ctx* c);
+void launch_dss_copy(ib3d_ctx* c);
+void launch_initial(ib3d_ctx* c);
+// k_momentum.cu
+void launch_momentum(ib3d_ctx* c);
+// k_ib.cu
+int run_surface_norm(ib3d_ctx* c);
+int run_search(ib3d_ctx* c);
+int run_velocity_forcing(ib3d_ctx* c);
+int run_pressure_forcing(ib3d_ctx* c);
+int run_stress(ib3d_ctx* c, int first, double coef[4]);
+
+// error helper: records the message and returns IB3D_ERR_CUDA
+int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where);
+}  // namespace ib3d
+
+#define IB3D_CUDA(c, expr)                                            \
+  do {                                                                \
+    cudaError_t _e = (expr);                                          \
+    if (_e != cudaSuccess) return ib3d::cuda_fail((c), _e, #expr);    \
+  } while (0)
+
+// ---- device helpers ----
+namespace ib3d {
+// max that keeps a NaN (fmax would drop it), so that a NaN in a convergence
+// scalar reaches the host check instead of reading as "converged".
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return (a != a) ? a : ((b > a || b != b) ? b : a);
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+// Block-wide max of a non-negative double, then one atomicMax on its bit pattern
+// (for non-negative IEEE doubles the integer order equals the numeric order).
+__device__ __forceinline__ void block_max_atomic(double v, unsigned long long* slot) {
+  __shared__ double sm[32];
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sm[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (int)((blockDim.x * blockDim.y * blockDim.z + 31) >> 5);
+    double x = lane < nw ? sm[lane] : 0.0;
+    x = warp_max(x);
+    if (lane == 0 && !(x <= 0.0)) atomicMax(slot, (unsigned long long)__double_as_longlong(x));
+  }
+}
+__device__ __forceinline__ double bits_to_double(unsigned long long b) { return __longlong_as_double((long long)b); }
+}  // namespace ib3d

@@ -1,0 +1,151 @@
+/*
+ * ib3d.h -- C ABI of the GB300 hot path of the IB3D sharp-interface immersed-
+ * boundary Navier-Stokes solver.
+ *
+ * The reference (Fortran 90 + OpenACC) runs its per-step hot path as
+ * argument-less subroutines over the module `global` (modGlobal.f90:1-106),
+ * called from PROGRAM main (main.f90:5-67). Each entry point below replaces one
+ * of those calls; the comment beside it names the reference interface
+ * (file:line) it stands in for. A Fortran driver binds them with ISO_C_BINDING
+ * (`bind(C)` interfaces) and replaces `CALL nsMomentum` by
+ * `ierr = ib3d_ns_momentum(ctx)`, and so on.
+ *
+ * Types: int64_t is Fortran INTEGER(KIND=8), double is REAL(KIND=8).
+ * 3-D arrays are the address of element (1,1,1) of a Fortran array with
+ * dimensions (nx+2, ny+2, nz+2), column-major (i fastest). Index lists are
+ * (n,3) INTEGER(8) column-major, 1-based.
+ *
+ * Ownership: the context owns all device memory; host pointers are only read or
+ * written for the duration of the call. Errors: every int-returning call
+ * returns IB3D_OK (0) or a negative IB3D_ERR_* code, and ib3d_last_error()
+ * describes it; nothing aborts, traps or loops forever. Threading: one context
+ * per host thread; work is ordered on the context's CUDA stream and a call
+ * synchronises only when it returns host data.
+ */
+#ifndef IB3D_H
+#define IB3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IB3D_OK 0
+#define IB3D_ERR_ARG (-1)       /* bad argument / call order */
+#define IB3D_ERR_CUDA (-2)      /* CUDA runtime error or missing device */
+#define IB3D_ERR_MESH (-3)      /* bad triangle index or degenerate mesh */
+#define IB3D_ERR_PROBE (-4)     /* a ghost-point or drag probe left the grid */
+#define IB3D_ERR_NOCONV (-5)    /* SOR hit max_sweeps; fields stay valid */
+#define IB3D_ERR_NONFINITE (-6) /* NaN or Inf in a convergence scalar */
+#define IB3D_ERR_MEMORY (-7)    /* device allocation failed */
+
+/* SOR stopping test. */
+#define IB3D_CRIT_UPDATE 0   /* max |pc - pco| over fluid cells (subPcorVcor.f90:193-210) */
+#define IB3D_CRIT_RESIDUAL 1 /* max |b/dt - A pc| over fluid cells */
+
+/* Pressure-solve arithmetic. */
+#define IB3D_PREC_FP64 0     /* reference arithmetic, bit-identical to the FP64 oracle */
+#define IB3D_PREC_FP32DC 1   /* FP32 red-black sweeps inside an FP64 defect-correction loop */
+
+/* Initial guess of the pressure correction pc at each step. */
+#define IB3D_WARM_ZERO 0     /* pc = 0, as subPcorVcor.f90:19-28 */
+#define IB3D_WARM_PREV 1     /* pc = previous step's pc (linear extrapolation of p) */
+
+typedef struct ib3d_params {
+  double re;            /* Reynolds number (inputdata line 2; rev = 1/re, subReadInput.f90:22) */
+  double deltat;        /* time step (subReadInput.f90:24) */
+  double omega;         /* SOR relaxation factor (reference hard-codes 1.99, subPcorVcor.f90:158) */
+  double eps;           /* SOR tolerance (inputdata eps1) */
+  int64_t max_sweeps;   /* sweep cap; the reference has none (pcItaMax is read but unused) */
+  int32_t criterion;    /* IB3D_CRIT_* */
+  int32_t precision;    /* IB3D_PREC_* */
+  int32_t warm_start;   /* IB3D_WARM_* */
+  int32_t check_every;  /* sweeps between residual checks (IB3D_CRIT_RESIDUAL); >= 1 */
+  int32_t inner_sweeps; /* FP32 sweeps per defect-correction pass (IB3D_PREC_FP32DC) */
+  int32_t reserved;
+} ib3d_params;
+
+/* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
+typedef struct ib3d_solve_stats {
+  int64_t sweeps;        /* nIterPcor: SOR sweeps (FP64 sweeps, or FP32 inner sweeps) */
+  int64_t outer;         /* defect-correction passes (0 for IB3D_PREC_FP64) */
+  double divmax;         /* max |div u*| over fluid cells before the solve */
+  double derr_std_st;    /* max |u_new - u_old| / dt over fluid cells */
+  double final_err;      /* last value of the stopping test */
+  double solve_seconds;  /* device time of the SOR loop (cpu_time pair at :33,:37) */
+} ib3d_solve_stats;
+
+typedef struct ib3d_ctx ib3d_ctx;
+
+/* Fills p with the reference's defaults (omega 1.99, eps 1e-5, update criterion). */
+void ib3d_default_params(ib3d_params* p);
+
+/* Grid and solver set-up: replaces readInput (subReadInput.f90:2-133), allocateArrays
+ * (subAllocateArrays.f90:1-15), coefficientMatrix (subCoefficientMatrix.f90:1-59) and
+ * non_uni_coeff (subNavierStokes.f90:3-619). x1n/y1n/z1n are the nx+1/ny+1/nz+1 node
+ * coordinates of gridx/y/z.dat. Selects device 0 if no device is current. */
+int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, int64_t nz,
+                const double* x1n, const double* y1n, const double* z1n);
+void ib3d_destroy(ib3d_ctx* ctx);
+const char* ib3d_last_error(const ib3d_ctx* ctx);
+/* Replaces the solver options of a live context (for example to switch precision). */
+int ib3d_set_params(ib3d_ctx* ctx, const ib3d_params* prm);
+
+/* Surface mesh: the arrays readSurfaceMeshGmsh fills (subReadInput.f90:137-176), then
+ * shiftSurfaceNodesInitial (subSearch.f90:2-39) and computeSurfaceNorm (subSearch.f90:80-131).
+ * e1/e2/e3 are 1-based node indices; inor is the normal orientation (+1 outward). */
+int ib3d_set_mesh(ib3d_ctx* ctx, int64_t nnodes, const double* xn, const double* yn, const double* zn,
+                  int64_t nelems, const int64_t* e1, const int64_t* e2, const int64_t* e3,
+                  double xshift, double yshift, double zshift, int64_t inor);
+
+/* tagging (subSearch.f90:134-321), cellCount (subSearch.f90:515-596) and
+ * computeNormDistance (subSearch.f90:599-678), plus the ghost-point schedule.
+ * box = {i_start, i_end, j_start, j_end, k_start, k_end} (inputdata lines 8-10).
+ * counts (may be NULL) = {fluid, solid, ib, red, black}. */
+int ib3d_search(ib3d_ctx* ctx, const int64_t box[6], int64_t counts[5]);
+
+/* Parity read-back of the search: cell flags (nx+2,ny+2,nz+2) int64 as in `cell`
+ * (modGlobal.f90:25), interceptedIndexPtr (nib,3), nelp (nib) and the seven normal
+ * distances (7 x nib: p, u1, u2, v1, v2, w1, w2). Any pointer may be NULL. */
+int ib3d_get_search(ib3d_ctx* ctx, int64_t* cell, int64_t* ib_list, int64_t* nelp, double* normdis);
+
+/* initialConditions (subInitialConditions.f90:2-48): all fields 0, u = 1 on fluid cells. */
+int ib3d_initial_conditions(ib3d_ctx* ctx);
+
+/* `!$acc update device` of the fields (subInitialConditions.f90:44, subLastConditions.f90:40).
+ * Any pointer may be NULL to leave that field unchanged. ut/vt/wt are set equal to u/v/w. */
+int ib3d_upload_fields(ib3d_ctx* ctx, const double* u, const double* v, const double* w, const double* p);
+/* `!$acc update host (u, v, w, ut, vt, wt, p, cell)` (main.f90:55). Any pointer may be NULL. */
+int ib3d_download_fields(ib3d_ctx* ctx, double* u, double* v, double* w, double* ut, double* vt,
+                         double* wt, double* p);
+/* Read back one device field: 0 u,1 v,2 w,3 ut,4 vt,5 wt,6 p,7 pc,8 b. */
+int ib3d_get_field(ib3d_ctx* ctx, int which, double* out);
+/* Write one device field (same numbering); for tests that start a routine from a given state. */
+int ib3d_set_field(ib3d_ctx* ctx, int which, const double* in);
+
+/* Per-step routines, in main.f90's order (:46-52). */
+int ib3d_ns_momentum(ib3d_ctx* ctx);      /* nsMomentum, subNavierStokes.f90:622-1122 */
+int ib3d_velocity_bc(ib3d_ctx* ctx);      /* velocityBC, subBoundaryConditions.f90:2-195 */
+int ib3d_solid_cell_bc(ib3d_ctx* ctx);    /* solidCellBC, subBoundaryConditions.f90:199-217 */
+int ib3d_velocity_forcing(ib3d_ctx* ctx); /* velocityForcing1, subForcing.f90:107-652 */
+int ib3d_pressure_forcing(ib3d_ctx* ctx); /* pressureForcing1, subForcing.f90:2-103 */
+/* poissonSolver, subPcorVcor.f90:2-80 (computeDiv, REDBLACKSOR, correctPressure,
+ * correctVelocity, velocityBC, steady-state indicator, u = ut). stats may be NULL. */
+int ib3d_poisson_solver(ib3d_ctx* ctx, ib3d_solve_stats* stats);
+/* stressCal1 (first != 0, subStressCal1.f90:2-460) or stressCal2 (subStressCal2.f90:2-381):
+ * coef = {Cd viscous, Cd pressure, Cl viscous, Cl pressure} (dragcoff.dat / liftcoff.dat). */
+int ib3d_stress(ib3d_ctx* ctx, int first, double coef[4]);
+/* The whole step of main.f90:42-66 (first selects stressCal1). stats/coef may be NULL. */
+int ib3d_step(ib3d_ctx* ctx, int first, ib3d_solve_stats* stats, double coef[4]);
+
+/* Device pointer of a field (same numbering as ib3d_get_field), for callers that keep
+ * data on the GPU; valid until ib3d_destroy. */
+void* ib3d_device_field(ib3d_ctx* ctx, int which);
+/* Blocks until the context's stream is idle. */
+int ib3d_synchronize(ib3d_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

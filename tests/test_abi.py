@@ -1,0 +1,58 @@
+"""CPU checks of the drop-in boundary: libib3d.so loads and exports every
+function include/ib3d.h declares, and fails cleanly (an error code, no crash)
+when no GPU is present."""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def built_lib(ib3d):
+    if not ib3d.LIB_PATH.exists():
+        ib3d.build()
+    return ib3d.LIB_PATH
+
+
+def test_header_declares_the_step_routines(ib3d):
+    names = ib3d.header_functions()
+    for n in ("ib3d_create", "ib3d_ns_momentum", "ib3d_velocity_bc", "ib3d_solid_cell_bc", "ib3d_velocity_forcing",
+              "ib3d_pressure_forcing", "ib3d_poisson_solver", "ib3d_stress", "ib3d_step", "ib3d_search",
+              "ib3d_set_mesh", "ib3d_destroy", "ib3d_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(ib3d, built_lib):
+    lib = ctypes.CDLL(str(built_lib))
+    missing = [n for n in ib3d.header_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_python_mirror_binds_every_symbol(ib3d, built_lib):
+    L = ib3d.lib()
+    for n in ib3d.header_functions():
+        assert getattr(L, n).argtypes is not None or getattr(L, n).restype is not None, n
+
+
+def test_params_struct_layout(ib3d, built_lib):
+    p = ib3d.default_params()
+    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6
+    assert p.omega == 1.99 and p.eps == 1e-5 and p.criterion == ib3d.CRIT_UPDATE
+
+
+def test_create_without_gpu_returns_error(ib3d, built_lib, grids):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    cs = grids.case("tiny")
+    with pytest.raises(ib3d.IB3DError) as e:
+        ib3d.Solver(cs.x, cs.y, cs.z, ib3d.default_params())
+    assert e.value.code == ib3d.ERR_CUDA
+
+
+def test_oracle_library_builds_and_loads(oracle_mod):
+    L = oracle_mod.lib()
+    for n in ("or_create", "or_step", "or_search", "or_poisson_solver", "or_stress"):
+        assert hasattr(L, n)

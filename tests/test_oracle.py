@@ -1,0 +1,159 @@
+"""CPU tests of the inputs and of the FP64 oracle: known-answer and analytic
+checks that pin the oracle, since the reference ships no tests or fixtures and
+cannot be run (no Fortran compiler)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def test_stretched_axis_fills_domain(grids):
+    nodes, rl, rr = grids.stretched_axis(-5.0, 15.0, 256, -0.8, 0.8, 1.0 / 40)
+    assert nodes.size == 257 and nodes[0] == -5.0 and nodes[-1] == 15.0
+    d = np.diff(nodes)
+    assert np.all(d > 0)
+    core = d[(nodes[:-1] >= -0.8 - 1e-12) & (nodes[1:] <= 0.8 + 1e-12)]
+    assert core.size == 64 and np.allclose(core, 1.0 / 40, rtol=0, atol=1e-14)
+    assert rl > 1.0 and rr > 1.0
+    # geometric growth away from the core on the high side
+    hi = d[nodes[:-1] >= 0.8 - 1e-12]
+    assert np.allclose(hi[1:-1] / hi[:-2], rr, rtol=1e-9)
+
+
+def test_stretch_ratio_solves_side():
+    from importlib import import_module
+    g = import_module("ib3d_gpu_gb300.grids")
+    r = g.solve_ratio(44, 0.025, 4.2)
+    assert abs(0.025 * sum(r ** m for m in range(1, 45)) - 4.2) < 1e-9
+
+
+def test_icosphere_counts_orientation_and_closure(grids):
+    nodes, tris = grids.icosphere(4, 0.5)
+    assert nodes.shape == (2562, 3) and tris.shape == (5120, 3)
+    assert tris.min() == 1 and tris.max() == 2562
+    assert np.allclose(np.linalg.norm(nodes, axis=1), 0.5, atol=1e-15)
+    p = nodes[tris - 1]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    c = p.mean(axis=1)
+    assert np.all(np.einsum("ij,ij->i", n, c) > 0), "triangles must wind outward"
+    edges = {}
+    for a, b, cc in tris:
+        for e in ((a, b), (b, cc), (cc, a)):
+            edges[tuple(sorted(e))] = edges.get(tuple(sorted(e)), 0) + 1
+    assert set(edges.values()) == {2}, "closed surface: every edge shared by two triangles"
+
+
+def test_gmsh_round_trip(grids, tmp_path):
+    nodes, tris = grids.icosphere(2, 0.5)
+    f = tmp_path / "sphere.msh"
+    grids.write_gmsh(f, nodes, tris)
+    n2, t2 = grids.read_gmsh(f)
+    assert np.array_equal(t2, tris) and np.array_equal(n2, nodes)
+
+
+def _uniform_oracle(oracle_mod, n=12, h=0.5):
+    x = np.arange(n + 1) * h
+    return oracle_mod.Oracle(x, x.copy(), x.copy(), re=100.0, deltat=0.01)
+
+
+def test_convection_coefficients_uniform_grid(oracle_mod):
+    """On a uniform grid the third-order upwind stencil of non_uni_coeff reduces to
+    u*(-u2+8u1-8um1+um2)/(12h) + |u|*(u2-4u1+6u0-4um1+um2)/(4h): the integer tables
+    below, exact in FP64 (subNavierStokes.f90:36-116)."""
+    o = _uniform_oracle(oracle_mod)
+    ca = [o.conv_coef(0, m)[5] for m in range(6)]
+    ck = [o.conv_coef(0, 6 + m)[5] for m in range(6)]
+    assert ca == [8640.0, -69120.0, 0.0, 69120.0, -8640.0, -103680.0]
+    assert ck == [2.0, -8.0, 12.0, -8.0, 2.0, 4.0]
+    for fam in range(6):
+        assert [o.conv_coef(fam, m)[4] for m in range(6)] == ca
+
+
+def test_poisson_coefficients_exact_for_quadratics(oracle_mod, grids):
+    """The 3-point operator of coefficientMatrix (subCoefficientMatrix.f90:8-33) is
+    exact for quadratics on any spacing: A applied to x^2 gives 2 on interior rows."""
+    nodes, _, _ = grids.stretched_axis(-2.0, 3.0, 20, -0.5, 0.5, 0.125)
+    o = oracle_mod.Oracle(nodes, nodes.copy(), nodes.copy(), re=100.0, deltat=0.01)
+    A = o.acoef(0)
+    xp = o.grid1d(15, o.nx + 3)
+    f = xp ** 2
+    for i in range(3, o.nx + 1):   # interior rows without folded boundary terms
+        val = A[i - 2, 0] * f[i - 1] + A[i - 2, 1] * f[i] + A[i - 2, 2] * f[i + 1]
+        assert abs(val - 2.0) < 1e-9
+    # boundary folding: inlet Neumann, outlet Dirichlet (x); Neumann both ends (y)
+    Ay = o.acoef(1)
+    assert A[0, 0] == 0.0 and A[-1, 2] == 0.0 and Ay[0, 0] == 0.0 and Ay[-1, 2] == 0.0
+
+
+def test_uniform_flow_is_steady_under_momentum(oracle_mod, grids):
+    """u = 1, v = w = p = 0 is a steady solution: the convection stencils sum to zero
+    and diffusion vanishes, so ut = 1 away from the boundary layer of ghost cells."""
+    cs = grids.case("tiny")
+    o = oracle_mod.Oracle(cs.x, cs.y, cs.z, cs.re, cs.dt)
+    nodes, tris = grids.icosphere(1, 0.1, centre=(4.0, 2.0, 2.0))
+    o.set_mesh(nodes, tris)
+    o.search((2, 3, 2, 3, 2, 3))   # a box without the body: every cell is fluid
+    assert o.counts["solid"] == 0 and o.counts["ib"] == 0
+    o.initial_conditions()
+    o.ns_momentum()
+    ut = o.get_field("ut")
+    inner = ut[4:-4, 4:-4, 4:-4]
+    assert np.max(np.abs(inner - 1.0)) < 1e-12
+
+
+def test_search_of_centred_sphere_is_symmetric(oracle_mod, grids):
+    """A sphere centred in a grid symmetric in y and z gives flags symmetric under
+    y -> -y and z -> -z up to the mesh's own asymmetry (the icosphere is not
+    mirror-symmetric), and solid cells lie inside the sphere, fluid cells outside."""
+    cs = grids.case("tiny")
+    o = oracle_mod.setup_case(cs)
+    s = o.get_search()
+    cell = s["cell"]
+    xp, yp, zp = (o.grid1d(q, n + 3)[1:n + 3] for q, n in ((15, o.nx), (16, o.ny), (17, o.nz)))
+    X, Y, Z = np.meshgrid(xp, yp, zp, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    assert np.all(r[cell == 1] < cs.radius)
+    assert np.all(r[cell == 2] < cs.radius + 0.2)
+    flagged = cell[1:-1, 1:-1, 1:-1]
+    mirrored = flagged[:, ::-1, :]
+    assert np.mean(flagged == mirrored) > 0.999
+    c = o.counts
+    assert c["fluid"] + c["solid"] + c["ib"] == o.nx * o.ny * o.nz
+    assert c["red"] + c["black"] == c["fluid"]
+    ib = s["ib"]
+    # lexicographic order (k outer, j, i inner), as cellCount builds it
+    key = ib[:, 2] * 10 ** 8 + ib[:, 1] * 10 ** 4 + ib[:, 0]
+    assert np.all(np.diff(key) > 0)
+
+
+def test_sor_solution_meets_residual_tolerance(oracle_mod, grids):
+    """After the residual-criterion solve, the numpy residual b/dt - A pc is below
+    eps on fluid cells and pc is zero off the fluid cells (Dirichlet at the body)."""
+    cs = grids.case("tiny")
+    o = oracle_mod.setup_case(cs, criterion=1, eps=1e-9, check_every=1)
+    o.ns_momentum(); o.velocity_bc(); o.solid_cell_bc(); o.velocity_forcing(); o.velocity_bc()
+    st = o.poisson_solver()
+    assert st["final_err"] < 1e-9
+    pc, b = o.get_field("pc"), o.get_field("b")
+    cell = o.get_search()["cell"]
+    A = [o.acoef(a) for a in range(3)]
+    nx, ny, nz = o.nx, o.ny, o.nz
+    sl = (slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1))
+    ax = lambda c: A[0][:, c][:, None, None]
+    ay = lambda c: A[1][:, c][None, :, None]
+    az = lambda c: A[2][:, c][None, None, :]
+    r = (b[sl] / cs.dt - ax(0) * pc[0:nx, 1:ny + 1, 1:nz + 1] - ax(2) * pc[2:nx + 2, 1:ny + 1, 1:nz + 1]
+         - ay(0) * pc[1:nx + 1, 0:ny, 1:nz + 1] - ay(2) * pc[1:nx + 1, 2:ny + 2, 1:nz + 1]
+         - az(0) * pc[1:nx + 1, 1:ny + 1, 0:nz] - az(2) * pc[1:nx + 1, 1:ny + 1, 2:nz + 2]
+         - (ax(1) + ay(1) + az(1)) * pc[sl])
+    fluid = cell[sl] == 0
+    assert np.max(np.abs(r[fluid])) < 1e-9 * 1.0001
+    assert np.all(pc[sl][~fluid] == 0.0)
+
+
+def test_sor_noconv_cap(oracle_mod, grids):
+    cs = grids.case("tiny")
+    o = oracle_mod.setup_case(cs, max_sweeps=7)
+    o.ns_momentum(); o.velocity_bc(); o.solid_cell_bc(); o.velocity_forcing(); o.velocity_bc()
+    st = o.poisson_solver(allow_noconv=True)
+    assert st["rc"] == 1 and st["sweeps"] == 7
