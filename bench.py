@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the IB3D per-time-step hot path on one GB300.
+
+Workload (sphere256): flow past a fixed sphere (icosphere D = 1, 2562 nodes,
+5120 triangles) at Re 300 on a 256x192x192 non-uniform staggered grid
+(D/40 uniform core on [-0.8,0.8]^3, geometric stretching to the domain
+[-5,15]x[-5,5]x[-5,5]), dt = 0.002, impulsive start u = 1. Each step is the
+reference's full step (momentum predictor, boundary conditions, ghost-point
+forcing, red-black SOR pressure solve with relaxation 1.99 to an FP64 residual
+L-inf <= 1e-6, pressure/velocity correction, drag/lift).
+
+value  = steps/s of the fast form: FP32 red-black sweeps inside an FP64
+         defect-correction loop, warm-started from the previous step's
+         correction, stopped at the same FP64 residual as the plain path.
+plain  = steps/s of the plain FP64 path (reference arithmetic, zero initial
+         correction) over the same physical steps.
+e2e    = the fast form through the C ABI with host buffers: the state is
+         uploaded from pinned host memory at the start of the timed region and
+         every step downloads u,v,w,ut,vt,wt,p to pinned host memory, as the
+         reference's per-step `update host` (main.f90:55) does.
+cpu_baseline / --impl reference = the FP64 oracle (the reference's algorithm
+         restated in C, OpenMP on all host cores), timed on a bounded sample
+         and scaled to steps/s (see `sample`).
+
+Timing: W untimed warm-up steps, then K steps between CUDA events recorded on
+the library's own stream, with a barrier and synchronize on both sides; every
+step reads and writes seven FP64 fields of 77.7 MB, so the inputs of each timed
+step are larger than the 129 MB L2.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+METRIC = "steps/s at 256×192×192 sphere: learned+FP32 vs plain FP64, residual ≤1e-6"
+BYTES_SOR32 = 13.0   # algorithmic bytes per cell of one FP32 red+black sweep: e 4 r + r 4 + e 4 w + flag 1
+BYTES_SOR64 = 25.0   # FP64 sweep: pc 8 r + b 8 + pc 8 w + flag 1
+
+
+def package():
+    if "ib3d_gpu_gb300" in sys.modules:
+        return sys.modules["ib3d_gpu_gb300"]
+    pkg = ROOT / "ib3d-gpu_gb300"
+    spec = importlib.util.spec_from_file_location("ib3d_gpu_gb300", pkg / "__init__.py",
+                                                  submodule_search_locations=[str(pkg)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["ib3d_gpu_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload(pkg, name: str):
+    cs = pkg.grids.case(name)
+    cs.omega = 1.99     # the reference's relaxation factor (subPcorVcor.f90:158)
+    cs.eps = 1e-6
+    return cs
+
+
+FAST = dict(precision=1, warm_start=1, criterion=1, inner_sweeps=128, max_sweeps=400000)
+PLAIN = dict(precision=0, warm_start=0, criterion=1, check_every=8, max_sweeps=400000)
+SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = [ln.split(",") for ln in open(self.f.name).read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[0])); mx.append(float(r[1])); pw.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for q, n in enumerate(names):
+                if len(r) > 4 + q and r[4 + q].strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------ distributed
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# -------------------------------------------------------------- GPU arms
+
+def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bool = True, clocks=None):
+    import torch
+    s = pkg.setup_case(cs, **mode)
+    first = True
+    for _ in range(warmup):
+        s.step(first)
+        first = False
+    s.synchronize()
+    if timers:
+        s.timers_enable(True)
+    stream = torch.cuda.ExternalStream(s.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    torch.cuda.nvtx.range_push("ib3d_timed")
+    e0.record(stream)
+    stats, coef = [], None
+    for _ in range(steps):
+        st, coef = s.step(first)
+        first = False
+        stats.append(st)
+    e1.record(stream)
+    torch.cuda.nvtx.range_pop()
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    dist.barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    tm = s.timers_read() if timers else None
+    s.close()
+    return {"seconds": t, "stats": stats, "coef": list(map(float, coef)), "timers": tm, "clocks": clk}
+
+
+def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist):
+    """The fast form through the C ABI with pinned host buffers in the timed region."""
+    import torch
+    s = pkg.setup_case(cs, **mode)
+    first = True
+    for _ in range(warmup):
+        s.step(first)
+        first = False
+    shape, n3 = s.shape, s.shape[0] * s.shape[1] * s.shape[2]
+
+    def pinned():
+        return torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy().reshape(shape, order="F")
+
+    host_in = {f: pinned() for f in ("u", "v", "w", "p")}
+    host_out = {f: pinned() for f in ("u", "v", "w", "ut", "vt", "wt", "p")}
+    for f in host_in:
+        host_in[f][...] = s.get_field(f)
+    stream = torch.cuda.ExternalStream(s.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s.upload_fields(host_in["u"], host_in["v"], host_in["w"], host_in["p"])
+    for _ in range(steps):
+        s.step(first)
+        first = False
+        s.download_fields(host_out)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    s.close()
+    return {"seconds": t, "h2d": 4 * n3 * 8 / steps, "d2h": 7 * n3 * 8 + 4 * 8}
+
+
+# ---------------------------------------------------------- CPU baseline
+
+def sweep_table() -> list[int]:
+    if SWEEP_TABLE.exists():
+        return json.loads(SWEEP_TABLE.read_text())["sweeps"]
+    return []
+
+
+def cpu_sample(pkg, cs, sweeps_per_step: float, threads: int) -> dict:
+    """Times the FP64 oracle (the reference's algorithm) on two capped steps of the
+    workload and scales to steps/s: t_step = t_fixed + n * t_sweep, where t_sweep
+    and t_fixed come from steps capped at 8 and 24 sweeps, and n is the number of
+    sweeps the full FP64 solve takes per step (the FP64 GPU path is bit-identical to
+    the oracle, so its sweep counts are the oracle's)."""
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    from oracle import oracle
+    oracle.set_threads(threads)
+    s1, s2 = 8, 40
+    o = oracle.setup_case(cs, criterion=1, check_every=8, max_sweeps=1)
+    o.step(True, allow_noconv=True)          # first step: drag-probe search and thread start-up, untimed
+    o.set_solver(cs.omega, cs.eps, 1, s1, 8)
+    t0 = time.perf_counter()
+    o.step(False, allow_noconv=True)
+    t1 = time.perf_counter() - t0
+    o.set_solver(cs.omega, cs.eps, 1, s2, 8)
+    t0 = time.perf_counter()
+    o.step(False, allow_noconv=True)
+    t2 = time.perf_counter() - t0
+    o.close()
+    t_sweep = max((t2 - t1) / (s2 - s1), 1e-9)
+    t_fixed = max(t1 - s1 * t_sweep, 0.0)
+    t_step = t_fixed + sweeps_per_step * t_sweep
+    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": (f"FP64 oracle (C restatement of the reference, OpenMP {threads} threads) on the "
+                       f"{cs.name} workload: after one untimed step, 2 steps capped at {s1} and {s2} SOR sweeps gave "
+                       f"t_sweep={t_sweep * 1e3:.2f} ms and t_fixed={t_fixed:.3f} s per step, scaled to "
+                       f"{sweeps_per_step:.0f} sweeps per step (the FP64 path's count on the same steps)"),
+            "t_sweep_s": t_sweep, "t_fixed_s": t_fixed, "sample_seconds": t1 + t2}
+
+
+# ------------------------------------------------------------------ main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--case", default="sphere256")
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 arm")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--record-sweeps", type=int, default=0,
+                    help="write the FP64 sweep counts of the first N steps to oracle/sweeps_<case>.json")
+    ap.add_argument("--record-out", default=None, help="output path of --record-sweeps")
+    ap.add_argument("--arms", default="fast,plain,e2e,cpu",
+                    help="comma-separated subset of fast,plain,e2e,cpu (profiling runs use 'fast')")
+    args = ap.parse_args()
+    warmup = max(args.warmup, 3)
+    dist = Dist()
+    pkg = package()
+    cs = workload(pkg, args.case)
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        table = sweep_table()
+        window = table[warmup:warmup + args.steps] if len(table) >= warmup + args.steps else table
+        n = sum(window) / len(window) if window else 8000.0
+        cpu = cpu_sample(pkg, cs, n, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 / cpu["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: icosphere body, stretched grid, impulsive start",
+                "config": {"workload": f"{cs.name} {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]}, Re {cs.re:g}, "
+                                       f"dt {cs.dt:g}, RB-SOR omega {cs.omega:g} to FP64 residual <= {cs.eps:g}",
+                           "mode": "reference algorithm in FP64 on the host cores"},
+                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cpu["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        dist.close()
+        return
+
+    import torch
+    torch.cuda.set_device(dist.local)
+
+    if args.record_sweeps:
+        s = pkg.setup_case(cs, **PLAIN)
+        counts = []
+        for q in range(args.record_sweeps):
+            st, _ = s.step(q == 0)
+            counts.append(int(st["sweeps"]))
+            print(f"step {q + 1}: {st['sweeps']} sweeps", file=sys.stderr, flush=True)
+        s.close()
+        path = pathlib.Path(args.record_out) if args.record_out else ROOT / "oracle" / f"sweeps_{cs.name}.json"
+        path.write_text(json.dumps({"workload": cs.name, "mode": "FP64, zero warm start, residual every 8 sweeps",
+                                    "omega": cs.omega, "eps": cs.eps, "sweeps": counts}, indent=1) + "\n")
+        print(json.dumps({"recorded": str(path), "sweeps": counts}), flush=True)
+        return
+
+    clocks = Clocks(dist.local)
+    fast = run_arm(pkg, cs, FAST, warmup, args.steps, dist, timers=True, clocks=clocks)
+    t = dist.max(fast["seconds"])
+    value = dist.world * args.steps / t
+    tm = fast["timers"]
+    ncell = cs.cells
+    sweeps = sum(st["sweeps"] for st in fast["stats"])
+    t_sweep32 = tm["sor32_ms"] / max(tm["sweeps32"], 1) * 1e-3
+    achieved = BYTES_SOR32 * ncell / t_sweep32 / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    phase_total = sum(tm[f"{p}_ms"] for p in pkg.Timers.PHASES)
+
+    arms = set(args.arms.split(","))
+    plain_steps = max(1, min(args.plain_steps, args.steps))
+    if "plain" in arms:
+        plain = run_arm(pkg, cs, PLAIN, warmup, plain_steps, dist, timers=True)
+        t_plain = dist.max(plain["seconds"])
+        plain_value = dist.world * plain_steps / t_plain
+        ptm = plain["timers"]
+        plain_sweeps = [st["sweeps"] for st in plain["stats"]]
+        t_sweep64 = ptm["sor64_ms"] / max(ptm["sweeps64"], 1) * 1e-3
+    else:
+        table = sweep_table()
+        plain_value, t_sweep64 = None, None
+        plain_sweeps = table[warmup:warmup + plain_steps] or [0]
+
+    if "e2e" in arms:
+        e2e = run_e2e(pkg, cs, FAST, warmup, args.steps, dist)
+        e2e_value = dist.world * args.steps / dist.max(e2e["seconds"])
+    else:
+        e2e, e2e_value = {"h2d": None, "d2h": None}, None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64",
+        "data": "synthetic: icosphere body (2562 nodes, 5120 triangles), stretched grid, impulsive start u=1",
+        "config": {"workload": f"{cs.name}: {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]} non-uniform grid, sphere D=1, "
+                               f"Re {cs.re:g}, dt {cs.dt:g}, red-black SOR omega {cs.omega:g} to FP64 residual "
+                               f"L-inf <= {cs.eps:g}",
+                   "mode": "FP32 red-black sweeps inside FP64 defect correction, warm start from the previous "
+                           "step's correction (learned warm start not in this line)",
+                   "inner_sweeps": FAST["inner_sweeps"],
+                   "l2": "inputs larger than L2: each step reads/writes 7 FP64 fields of 77.7 MB",
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "plain_fp64": {"value": plain_value, "unit": "steps/s", "steps": plain_steps,
+                       "sweeps_per_step": sum(plain_sweeps) / len(plain_sweeps),
+                       "ms_per_sweep": t_sweep64 * 1e3 if t_sweep64 else None,
+                       "sweep_bound": "FP64 ALU (GB300 FP64 ~0.5 TFMA/s measured)"},
+        "speedup_vs_plain_fp64": value / plain_value if plain_value else None,
+        "sweeps_per_step": sweeps / args.steps,
+        "sweeps_per_s": tm["sweeps32"] / (tm["sor32_ms"] * 1e-3) if tm["sor32_ms"] else None,
+        "cells_per_s": value * ncell,
+        "phase_ms_per_step": {p: tm[f"{p}_ms"] / args.steps for p in pkg.Timers.PHASES},
+        "drag_lift": fast["coef"],
+        "roofline": {"kernel": "k_sor32 (one FP32 red+black sweep)", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "bytes_per_cell": BYTES_SOR32, "cells": ncell, "ms_per_launch": t_sweep32 * 1e3,
+                     "share_of_step": tm["sor32_ms"] / phase_total if phase_total else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"]},
+        "gpu_launches": tm["launches"],
+        "clocks": fast["clocks"],
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu and "cpu" in arms:
+        cpu = cpu_sample(pkg, cs, sum(plain_sweeps) / len(plain_sweeps), threads)
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -46,7 +46,7 @@ class Params(C.Structure):
     _fields_ = [("re", C.c_double), ("deltat", C.c_double), ("omega", C.c_double), ("eps", C.c_double),
                 ("max_sweeps", C.c_int64), ("criterion", C.c_int32), ("precision", C.c_int32),
                 ("warm_start", C.c_int32), ("check_every", C.c_int32), ("inner_sweeps", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("sweep_kernel", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -55,6 +55,18 @@ class SolveStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Timers(C.Structure):
+    _fields_ = [("ms", C.c_double * 9), ("sweeps64", C.c_int64), ("sweeps32", C.c_int64), ("outer", C.c_int64),
+                ("launches", C.c_int64), ("steps", C.c_int64)]
+    PHASES = ("momentum", "bc", "forcing", "divergence", "sor64", "sor32", "residual", "correct", "stress")
+
+    def as_dict(self) -> dict:
+        d = {f"{n}_ms": self.ms[q] for q, n in enumerate(self.PHASES)}
+        for k in ("sweeps64", "sweeps32", "outer", "launches", "steps"):
+            d[k] = getattr(self, k)
+        return d
 
 
 _lib = None
@@ -102,6 +114,9 @@ def lib() -> C.CDLL:
         "ib3d_stress": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_step": (C.c_int, [_VP, C.c_int, C.POINTER(SolveStats), _D]),
         "ib3d_device_field": (_VP, [_VP, C.c_int]),
+        "ib3d_timers_enable": (C.c_int, [_VP, C.c_int]),
+        "ib3d_timers_read": (C.c_int, [_VP, C.POINTER(Timers)]),
+        "ib3d_stream": (_VP, [_VP]),
         "ib3d_synchronize": (C.c_int, [_VP]),
     }
     for name, (res, args) in sig.items():
@@ -234,6 +249,18 @@ class Solver:
 
     def synchronize(self):
         self._check(self.L.ib3d_synchronize(self._h), "ib3d_synchronize")
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return self.L.ib3d_stream(self._h) or 0
+
+    def timers_enable(self, on: bool = True):
+        self._check(self.L.ib3d_timers_enable(self._h, 1 if on else 0), "ib3d_timers_enable")
+
+    def timers_read(self) -> dict:
+        t = Timers()
+        self._check(self.L.ib3d_timers_read(self._h, C.byref(t)), "ib3d_timers_read")
+        return t.as_dict()
 
     # -- the reference's per-step calls (main.f90:46-66)
     def ns_momentum(self):

@@ -20,6 +20,37 @@ int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where) {
 
 void free_ib(ib3d_ctx* c);
 
+cudaEvent_t timer_event(ib3d_ctx* c) {
+  if (!c->pool.empty()) {
+    cudaEvent_t e = c->pool.back();
+    c->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+namespace {
+// Resolves the recorded event pairs into per-phase milliseconds.
+void timer_fold(ib3d_ctx* c) {
+  if (c->pending.empty()) return;
+  cudaStreamSynchronize(c->st);
+  for (auto& pr : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, pr.a, pr.b) == cudaSuccess) c->tms[pr.phase] += ms;
+    c->pool.push_back(pr.a);
+    c->pool.push_back(pr.b);
+  }
+  c->pending.clear();
+}
+}  // namespace
+
+void timer_push(ib3d_ctx* c, int phase, cudaEvent_t a, cudaEvent_t b) {
+  c->pending.push_back({phase, a, b});
+  if (c->pending.size() > 4096) timer_fold(c);
+}
+
 namespace {
 
 // One station of non_uni_coeff (subNavierStokes.f90:37-116): the 12 coefficients of
@@ -140,10 +171,12 @@ int alloc_fields(ib3d_ctx* c) {
     if (cudaMemsetAsync(*q, 0, n3 * sizeof(double), c->st) != cudaSuccess) return IB3D_ERR_CUDA;
   }
   if (cudaMalloc(&c->e32, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
+  if (cudaMalloc(&c->e32b, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->r32, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->cell, n3) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->ibmap, n3 * sizeof(int)) != cudaSuccess) return IB3D_ERR_MEMORY;
   cudaMemsetAsync(c->e32, 0, n3 * sizeof(float), c->st);
+  cudaMemsetAsync(c->e32b, 0, n3 * sizeof(float), c->st);
   cudaMemsetAsync(c->r32, 0, n3 * sizeof(float), c->st);
   cudaMemsetAsync(c->cell, 0, n3, c->st);
   cudaMemsetAsync(c->ibmap, 0xff, n3 * sizeof(int), c->st);
@@ -161,7 +194,7 @@ bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
          (p->precision == 0 || p->precision == 1) && (p->warm_start == 0 || p->warm_start == 1) &&
-         p->check_every >= 1 && p->inner_sweeps >= 1;
+         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1);
 }
 
 int fail(ib3d_ctx* c, int code, const char* msg) {
@@ -316,9 +349,11 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
 void ib3d_destroy(ib3d_ctx* c) {
   if (!c) return;
   if (c->st) cudaStreamSynchronize(c->st);
+  timer_fold(c);
+  for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
   free_ib(c);
   void* ptrs[] = {c->d_tables, c->d_tables32, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
-                  c->e32, c->r32, c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
+                  c->e32, c->e32b, c->r32, c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -474,6 +509,33 @@ int ib3d_set_field(ib3d_ctx* c, int which, const double* in) {
 
 void* ib3d_device_field(ib3d_ctx* c, int which) { return c ? (void*)field_ptr(c, which) : nullptr; }
 
+void* ib3d_stream(ib3d_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int ib3d_timers_enable(ib3d_ctx* c, int on) {
+  if (!c) return IB3D_ERR_ARG;
+  timer_fold(c);
+  if (on) {
+    for (double& x : c->tms) x = 0.0;
+    c->t_sweeps64 = c->t_sweeps32 = c->t_outer = c->t_steps = 0;
+    c->launches = 0;
+  }
+  c->timing = on != 0;
+  return IB3D_OK;
+}
+
+int ib3d_timers_read(ib3d_ctx* c, ib3d_timers* out) {
+  if (!c || !out) return IB3D_ERR_ARG;
+  timer_fold(c);
+  IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  for (int q = 0; q < 9; ++q) out->ms[q] = c->tms[q];
+  out->sweeps64 = c->t_sweeps64;
+  out->sweeps32 = c->t_sweeps32;
+  out->outer = c->t_outer;
+  out->launches = c->launches;
+  out->steps = c->t_steps;
+  return IB3D_OK;
+}
+
 int ib3d_synchronize(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
   IB3D_CUDA(c, cudaStreamSynchronize(c->st));
@@ -565,6 +627,7 @@ int ib3d_step(ib3d_ctx* c, int first, ib3d_solve_stats* stats, double coef[4]) {
   if (!c) return IB3D_ERR_ARG;
   if (!c->searched) return fail(c, IB3D_ERR_ARG, "ib3d_step: call ib3d_search first");
   int rc;
+  c->t_steps += 1;
   if ((rc = ib3d_ns_momentum(c))) return rc;        // main.f90:46
   if ((rc = ib3d_velocity_bc(c))) return rc;        // :47
   if ((rc = ib3d_solid_cell_bc(c))) return rc;      // :48

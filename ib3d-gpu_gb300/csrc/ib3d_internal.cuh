@@ -98,7 +98,7 @@ struct ib3d_ctx {
   ib3d::Grid1D g{};
   double *u = nullptr, *v = nullptr, *w = nullptr, *ut = nullptr, *vt = nullptr, *wt = nullptr;
   double *p = nullptr, *pc = nullptr, *b = nullptr, *bdt = nullptr;
-  float *e32 = nullptr, *r32 = nullptr;
+  float *e32 = nullptr, *e32b = nullptr, *r32 = nullptr;
   unsigned char* cell = nullptr;
   int* ibmap = nullptr;
   ib3d::SolveCtl* ctl = nullptr;
@@ -133,6 +133,18 @@ struct ib3d_ctx {
   // reduction / scan scratch
   long long* d_scan = nullptr;
   size_t scan_cap = 0;
+
+  // phase timers (ib3d_timers_*) and the launch counter
+  bool timing = false;
+  struct EvPair {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<EvPair> pending;
+  std::vector<cudaEvent_t> pool;
+  double tms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  long long t_sweeps64 = 0, t_sweeps32 = 0, t_outer = 0, t_steps = 0;
+  long long launches = 0;
 };
 
 // ---- kernel launchers (defined in the .cu files) ----
@@ -148,6 +160,8 @@ void launch_dss_copy(ib3d_ctx* c);
 void launch_initial(ib3d_ctx* c);
 // k_momentum.cu
 void launch_momentum(ib3d_ctx* c);
+// k_sor32.cu
+void launch_sor32_fused(ib3d_ctx* c, const float* ein, float* eout, float omega, float om1);
 // k_ib.cu
 int run_surface_norm(ib3d_ctx* c);
 int run_search(ib3d_ctx* c);
@@ -157,6 +171,32 @@ int run_stress(ib3d_ctx* c, int first, double coef[4]);
 
 // error helper: records the message and returns IB3D_ERR_CUDA
 int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where);
+
+// Phase indices of ib3d_timers.ms
+enum Phase { PH_MOMENTUM = 0, PH_BC, PH_FORCING, PH_DIVERGENCE, PH_SOR64, PH_SOR32, PH_RESIDUAL, PH_CORRECT,
+             PH_STRESS };
+cudaEvent_t timer_event(ib3d_ctx* c);
+void timer_push(ib3d_ctx* c, int phase, cudaEvent_t a, cudaEvent_t b);
+// Records a start event on construction and an end event on destruction when the
+// context's timers are on; otherwise does nothing.
+struct PhaseScope {
+  ib3d_ctx* c;
+  int ph;
+  cudaEvent_t a = nullptr;
+  PhaseScope(ib3d_ctx* c_, int ph_) : c(c_), ph(ph_) {
+    if (c->timing) {
+      a = timer_event(c);
+      cudaEventRecord(a, c->st);
+    }
+  }
+  ~PhaseScope() {
+    if (a) {
+      cudaEvent_t b = timer_event(c);
+      cudaEventRecord(b, c->st);
+      timer_push(c, ph, a, b);
+    }
+  }
+};
 }  // namespace ib3d
 
 #define IB3D_CUDA(c, expr)                                            \

@@ -765,7 +765,9 @@ int run_search(ib3d_ctx* c) {
 }
 
 int run_velocity_forcing(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_FORCING);
   ForceSched& s = c->fv;
+  c->launches += s.nlevels + (s.nfinal > 0 ? 1 : 0);
   for (int l = 0; l < s.nlevels; ++l) {
     const int off = s.level_off[l], cnt = s.level_off[l + 1] - off;
     if (cnt <= 0) continue;
@@ -781,7 +783,9 @@ int run_velocity_forcing(ib3d_ctx* c) {
 }
 
 int run_pressure_forcing(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_FORCING);
   ForceSched& s = c->fp;
+  c->launches += s.nlevels + (s.nfinal > 0 ? 1 : 0);
   for (int l = 0; l < s.nlevels; ++l) {
     const int off = s.level_off[l], cnt = s.level_off[l + 1] - off;
     if (cnt <= 0) continue;
@@ -799,6 +803,8 @@ int run_stress(ib3d_ctx* c, int first, double coef[4]) {
   const int ne = (int)c->nelems;
   const int do_first = (first || !c->have_scache) ? 1 : 0;
   if (do_first) IB3D_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->st));
+  PhaseScope ps(c, PH_STRESS);
+  c->launches += 2;
   k_stress_elem<<<nblk(ne), kBlock, 0, c->st>>>(c->d, c->g, c->d_surf, ne, do_first, c->d_scache, c->ut, c->vt,
                                                 c->wt, c->p, 1.0 / c->prm.re, c->d_contrib, c->d_flag);
   k_stress_sum<<<1, 32, 0, c->st>>>(c->d_contrib, ne, c->d_coef);

@@ -165,6 +165,8 @@ __global__ void __launch_bounds__(128) k_momentum(Dims d, Grid1D g, const double
 }
 
 void launch_momentum(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_MOMENTUM);
+  c->launches += 1;
   const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;
   const unsigned nb = (unsigned)((n + 127) / 128);
   k_momentum<<<nb, 128, 0, c->st>>>(c->d, c->g, c->u, c->v, c->w, c->p, c->cell, c->ut, c->vt, c->wt,

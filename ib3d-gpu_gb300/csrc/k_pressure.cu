@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Dims d, Grid1D g, const d
     const unsigned t = tid / (unsigned)d.nx;
     const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
     const long long idx = d.at(i, j, k);
-    float rr = 0.0f;
+    float rr = __int_as_float(0x7fc00000);   // NaN marks a non-fluid cell for the FP32 sweep
     if (cell[idx] == 0) {
       const long long sy = d.NX2, sz = (long long)d.NX2 * d.NY2;
       const double num = bdt[idx] - g.acx[0][i - 1] * pc[idx - 1] - g.acx[2][i - 1] * pc[idx + 1] -
@@ -314,16 +314,22 @@ __global__ void k_initial(Dims d, const unsigned char* __restrict__ cell, double
 // ---------------------------------------------------------------- launchers
 
 void launch_divergence(ib3d_ctx* c, bool zero_pc) {
+  PhaseScope ps(c, PH_DIVERGENCE);
+  c->launches += 1;
   k_divergence<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d, c->g, c->ut, c->vt, c->wt, c->cell, c->b, c->bdt,
                                                         c->pc, c->prm.deltat, zero_pc ? 1 : 0, &c->ctl->aux);
 }
 
 void launch_correct(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_CORRECT);
+  c->launches += 1;
   const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;
   k_correct<<<nblocks(n), kBlock, 0, c->st>>>(c->d, c->g, c->pc, c->cell, c->p, c->ut, c->vt, c->wt);
 }
 
 void launch_velocity_bc(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_BC);
+  c->launches += 3;
   const Dims& d = c->d;
   k_bc_x<<<nblocks((long long)d.ny * d.nz), kBlock, 0, c->st>>>(d, c->ut, c->vt, c->wt);
   k_bc_y<<<nblocks((long long)d.nx * d.nz), kBlock, 0, c->st>>>(d, c->ut, c->vt, c->wt);
@@ -331,15 +337,20 @@ void launch_velocity_bc(ib3d_ctx* c) {
 }
 
 void launch_solid_bc(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_BC);
+  c->launches += 1;
   k_solid_bc<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d, c->cell, c->ut, c->vt, c->wt, c->p);
 }
 
 void launch_dss_copy(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_CORRECT);
+  c->launches += 1;
   k_dss_copy<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d, c->cell, c->u, c->v, c->w, c->ut, c->vt, c->wt,
                                                       c->prm.deltat, &c->ctl->aux);
 }
 
 void launch_initial(ib3d_ctx* c) {
+  c->launches += 1;
   k_initial<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d, c->cell, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p,
                                                      c->pc);
 }
@@ -375,8 +386,11 @@ int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st) {
   long long sweep = 0;
   long long batch = 4;
   for (;;) {
+    {
+    PhaseScope ps(c, PH_SOR64);
     for (long long q = 0; q < batch; ++q) {
       ++sweep;
+      c->launches += (resid && (sweep % every) == 0) ? 3 : 2;
       int mode_black = resid ? ((sweep % every) ? 1 : 2) : 0;
       k_sor64<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, P.omega, om1, c->ctl, sweep, 2,
                                              P.eps, P.max_sweeps);
@@ -386,6 +400,7 @@ int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st) {
         k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, nullptr, c->ctl,
                                                             sweep, 0, P.eps, P.max_sweeps);
     }
+    }
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);
     if (rc) return rc;
@@ -394,6 +409,7 @@ int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st) {
   }
   st->sweeps = c->h_ctl->nsweeps;
   st->outer = 0;
+  c->t_sweeps64 += st->sweeps;
   st->final_err = c->h_ctl->final_err;
   if (c->h_ctl->final_err != c->h_ctl->final_err) return IB3D_ERR_NONFINITE;
   return c->h_ctl->done == 2 ? IB3D_ERR_NOCONV : IB3D_OK;
@@ -418,22 +434,48 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
   long long sweeps = 0, outer = 0;
   for (;;) {
-    k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, c->r32, c->ctl, sweeps,
-                                                        0, P.eps, P.max_sweeps);
+    {
+      PhaseScope ps(c, PH_RESIDUAL);
+      c->launches += 1;
+      k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, c->r32, c->ctl, sweeps,
+                                                          0, P.eps, P.max_sweeps);
+    }
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);
     if (rc) return rc;
     if (c->h_ctl->done) break;
-    for (int q = 0; q < inner; ++q) {
-      k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
-      k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
+    {
+      PhaseScope ps(c, PH_SOR32);
+      if (P.sweep_kernel == 0) {
+        // one fused launch per sweep, ping-ponging between e32 and e32b
+        c->launches += inner;
+        float* ein = c->e32;
+        float* eout = c->e32b;
+        for (int q = 0; q < inner; ++q) {
+          launch_sor32_fused(c, ein, eout, om, om1);
+          float* t = ein; ein = eout; eout = t;
+        }
+        if (ein != c->e32) { c->e32b = c->e32; c->e32 = ein; }   // c->e32 holds the result
+      } else {
+        c->launches += 2 * inner;
+        for (int q = 0; q < inner; ++q) {
+          k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
+          k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
+        }
+      }
     }
-    k_accumulate<<<nblocks(d.n3), kBlock, 0, c->st>>>(d.n3, c->pc, c->e32);
+    {
+      PhaseScope ps(c, PH_RESIDUAL);
+      c->launches += 1;
+      k_accumulate<<<nblocks(d.n3), kBlock, 0, c->st>>>(d.n3, c->pc, c->e32);
+    }
     sweeps += inner;
     ++outer;
   }
   st->sweeps = c->h_ctl->nsweeps;
   st->outer = outer;
+  c->t_sweeps32 += sweeps;
+  c->t_outer += outer;
   st->final_err = c->h_ctl->final_err;
   if (c->h_ctl->final_err != c->h_ctl->final_err) return IB3D_ERR_NONFINITE;
   return c->h_ctl->done == 2 ? IB3D_ERR_NOCONV : IB3D_OK;

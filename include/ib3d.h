@@ -63,7 +63,7 @@ typedef struct ib3d_params {
   int32_t warm_start;   /* IB3D_WARM_* */
   int32_t check_every;  /* sweeps between residual checks (IB3D_CRIT_RESIDUAL); >= 1 */
   int32_t inner_sweeps; /* FP32 sweeps per defect-correction pass (IB3D_PREC_FP32DC) */
-  int32_t reserved;
+  int32_t sweep_kernel; /* FP32 sweep form: 0 one fused launch per sweep, 1 one launch per colour */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
@@ -138,6 +138,26 @@ int ib3d_poisson_solver(ib3d_ctx* ctx, ib3d_solve_stats* stats);
 int ib3d_stress(ib3d_ctx* ctx, int first, double coef[4]);
 /* The whole step of main.f90:42-66 (first selects stressCal1). stats/coef may be NULL. */
 int ib3d_step(ib3d_ctx* ctx, int first, ib3d_solve_stats* stats, double coef[4]);
+
+/* Phase timers (the reference times only its SOR loop with cpu_time,
+ * subPcorVcor.f90:33-37, and logs it to iter.dat :60-65). When enabled, every
+ * phase records CUDA events on the context's stream; reading synchronizes.
+ * ms[]: 0 momentum, 1 boundary conditions, 2 forcing, 3 divergence, 4 FP64 sweeps,
+ * 5 FP32 sweeps, 6 residual + accumulation, 7 corrections + copy, 8 drag/lift. */
+typedef struct ib3d_timers {
+  double ms[9];
+  int64_t sweeps64;   /* FP64 red-black sweeps run */
+  int64_t sweeps32;   /* FP32 red-black sweeps run */
+  int64_t outer;      /* defect-correction passes */
+  int64_t launches;   /* kernels launched by the library */
+  int64_t steps;      /* ib3d_step calls */
+} ib3d_timers;
+/* on != 0 clears and starts the timers; on == 0 stops them (counts are kept). */
+int ib3d_timers_enable(ib3d_ctx* ctx, int on);
+int ib3d_timers_read(ib3d_ctx* ctx, ib3d_timers* out);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work
+ * with the library's or record events on it. */
+void* ib3d_stream(ib3d_ctx* ctx);
 
 /* Device pointer of a field (same numbering as ib3d_get_field), for callers that keep
  * data on the GPU; valid until ib3d_destroy. */
