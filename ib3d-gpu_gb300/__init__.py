@@ -26,14 +26,14 @@ HERE = pathlib.Path(__file__).resolve().parent
 LIB_PATH = HERE / "libib3d.so"
 HEADER = HERE.parent / "include" / "ib3d.h"
 
-OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMORY = 0, -1, -2, -3, -4, -5, -6, -7
+OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMORY, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
 PREC_FP64, PREC_FP32DC = 0, 1
 WARM_ZERO, WARM_PREV = 0, 1
 FIELDS = {"u": 0, "v": 1, "w": 2, "ut": 3, "vt": 4, "wt": 5, "p": 6, "pc": 7, "b": 8}
 _ERRNAMES = {ERR_ARG: "IB3D_ERR_ARG", ERR_CUDA: "IB3D_ERR_CUDA", ERR_MESH: "IB3D_ERR_MESH",
              ERR_PROBE: "IB3D_ERR_PROBE", ERR_NOCONV: "IB3D_ERR_NOCONV", ERR_NONFINITE: "IB3D_ERR_NONFINITE",
-             ERR_MEMORY: "IB3D_ERR_MEMORY"}
+             ERR_MEMORY: "IB3D_ERR_MEMORY", ERR_TOO_LARGE: "IB3D_ERR_TOO_LARGE"}
 
 
 class IB3DError(RuntimeError):
@@ -117,6 +117,9 @@ def lib() -> C.CDLL:
         "ib3d_timers_enable": (C.c_int, [_VP, C.c_int]),
         "ib3d_timers_read": (C.c_int, [_VP, C.POINTER(Timers)]),
         "ib3d_stream": (_VP, [_VP]),
+        "ib3d_pressure_solve_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, _VP, _VP, _VP, _VP, _VP,
+                                                  C.c_double, _VP, C.c_double, C.c_double, C.c_int64, C.c_int32,
+                                                  _VP, _I64, _D]),
         "ib3d_synchronize": (C.c_int, [_VP]),
     }
     for name, (res, args) in sig.items():

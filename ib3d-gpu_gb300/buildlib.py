@@ -15,7 +15,7 @@ import subprocess
 HERE = pathlib.Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIB = HERE / "libib3d.so"
-SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu"]
+SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -39,6 +39,7 @@ extern "C" {
 #define IB3D_ERR_NOCONV (-5)    /* SOR hit max_sweeps; fields stay valid */
 #define IB3D_ERR_NONFINITE (-6) /* NaN or Inf in a convergence scalar */
 #define IB3D_ERR_MEMORY (-7)    /* device allocation failed */
+#define IB3D_ERR_TOO_LARGE (-8) /* grid larger than ib3d_pressure_solve_noalloc's fixed scratch */
 
 /* SOR stopping test. */
 #define IB3D_CRIT_UPDATE 0   /* max |pc - pco| over fluid cells (subPcorVcor.f90:193-210) */
@@ -164,6 +165,33 @@ void* ib3d_stream(ib3d_ctx* ctx);
 void* ib3d_device_field(ib3d_ctx* ctx, int which);
 /* Blocks until the context's stream is idle. */
 int ib3d_synchronize(ib3d_ctx* ctx);
+
+/* Mixed-precision pressure solve that allocates no memory. No counterpart in the
+ * reference: it serves host codes that cannot call cudaMalloc -- a solver whose
+ * device memory belongs to another runtime (an OpenACC data region, a framework's
+ * caching allocator, a fixed pool sized at start-up) or one that must not allocate
+ * inside its time loop. It needs no context: the caller passes every array as a
+ * device pointer it owns, and the FP32 work arrays and control block live in one
+ * static device array built into the library, which each GPU that loads the library
+ * holds until the process exits.
+ *
+ * Solves A pc = b/deltat on the fluid cells (cell == 0) by FP64 defect correction
+ * around inner_sweeps FP32 red-black sweeps per pass, from the pc given, until the
+ * FP64 residual L-inf drops below eps (IB3D_ERR_NOCONV after max_sweeps). acx/acy/acz
+ * are the (n,3) column-major Poisson coefficients of coefficientMatrix
+ * (subCoefficientMatrix.f90:1-59); cell, b and pc are (nx+2,ny+2,nz+2) arrays in the
+ * reference's layout (cell as uint8). stream is a cudaStream_t or NULL.
+ *
+ * Limit: (nx+2)*(ny+2)*(nz+2) <= 2^21 cells (two 8 MiB FP32 arrays); larger grids
+ * return IB3D_ERR_TOO_LARGE. The first call on a device looks up the scratch's device
+ * address (cudaGetSymbolAddress) and caches it; make that first call before any
+ * stream capture. Every call uses the same scratch and clears what must start at
+ * zero, so calls that overlap on the GPU (other streams, other host threads) race:
+ * serialise them. */
+int ib3d_pressure_solve_noalloc(int64_t nx, int64_t ny, int64_t nz, const double* acx, const double* acy,
+                                const double* acz, const unsigned char* cell, const double* b, double deltat,
+                                double* pc, double omega, double eps, int64_t max_sweeps, int32_t inner_sweeps,
+                                void* stream, int64_t* sweeps, double* residual);
 
 #ifdef __cplusplus
 }
