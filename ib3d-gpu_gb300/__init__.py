@@ -29,7 +29,7 @@ HEADER = HERE.parent / "include" / "ib3d.h"
 OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMORY, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
 PREC_FP64, PREC_FP32DC = 0, 1
-WARM_ZERO, WARM_PREV = 0, 1
+WARM_ZERO, WARM_PREV, WARM_LEARNED = 0, 1, 2
 FIELDS = {"u": 0, "v": 1, "w": 2, "ut": 3, "vt": 4, "wt": 5, "p": 6, "pc": 7, "b": 8}
 _ERRNAMES = {ERR_ARG: "IB3D_ERR_ARG", ERR_CUDA: "IB3D_ERR_CUDA", ERR_MESH: "IB3D_ERR_MESH",
              ERR_PROBE: "IB3D_ERR_PROBE", ERR_NOCONV: "IB3D_ERR_NOCONV", ERR_NONFINITE: "IB3D_ERR_NONFINITE",
@@ -46,7 +46,7 @@ class Params(C.Structure):
     _fields_ = [("re", C.c_double), ("deltat", C.c_double), ("omega", C.c_double), ("eps", C.c_double),
                 ("max_sweeps", C.c_int64), ("criterion", C.c_int32), ("precision", C.c_int32),
                 ("warm_start", C.c_int32), ("check_every", C.c_int32), ("inner_sweeps", C.c_int32),
-                ("sweep_kernel", C.c_int32)]
+                ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double)]
 
 
 class SolveStats(C.Structure):
@@ -58,9 +58,9 @@ class SolveStats(C.Structure):
 
 
 class Timers(C.Structure):
-    _fields_ = [("ms", C.c_double * 9), ("sweeps64", C.c_int64), ("sweeps32", C.c_int64), ("outer", C.c_int64),
+    _fields_ = [("ms", C.c_double * 10), ("sweeps64", C.c_int64), ("sweeps32", C.c_int64), ("outer", C.c_int64),
                 ("launches", C.c_int64), ("steps", C.c_int64)]
-    PHASES = ("momentum", "bc", "forcing", "divergence", "sor64", "sor32", "residual", "correct", "stress")
+    PHASES = ("momentum", "bc", "forcing", "divergence", "sor64", "sor32", "residual", "correct", "stress", "net")
 
     def as_dict(self) -> dict:
         d = {f"{n}_ms": self.ms[q] for q, n in enumerate(self.PHASES)}
@@ -72,6 +72,7 @@ class Timers(C.Structure):
 _lib = None
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
+_F = C.POINTER(C.c_float)
 _VP = C.c_void_p
 
 
@@ -117,6 +118,19 @@ def lib() -> C.CDLL:
         "ib3d_timers_enable": (C.c_int, [_VP, C.c_int]),
         "ib3d_timers_read": (C.c_int, [_VP, C.POINTER(Timers)]),
         "ib3d_stream": (_VP, [_VP]),
+        "ib3d_net_create": (C.c_int, [C.POINTER(_VP), C.c_uint64]),
+        "ib3d_net_destroy": (None, [_VP]),
+        "ib3d_net_last_error": (C.c_char_p, [_VP]),
+        "ib3d_net_num_params": (C.c_int64, [_VP]),
+        "ib3d_net_get_params": (C.c_int, [_VP, _F]),
+        "ib3d_net_set_params": (C.c_int, [_VP, _F]),
+        "ib3d_net_loss_grad": (C.c_int, [_VP, C.c_int, C.c_int, _F, _F, _D, _F, _F]),
+        "ib3d_net_dataset_reserve": (C.c_int, [_VP, C.c_int, C.c_int64]),
+        "ib3d_net_dataset_size": (C.c_int64, [_VP]),
+        "ib3d_net_capture": (C.c_int, [_VP, _VP, C.c_int, C.c_uint64]),
+        "ib3d_net_train": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_uint64, _D]),
+        "ib3d_enable_history": (C.c_int, [_VP]),
+        "ib3d_attach_net": (C.c_int, [_VP, _VP]),
         "ib3d_pressure_solve_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, _VP, _VP, _VP, _VP, _VP,
                                                   C.c_double, _VP, C.c_double, C.c_double, C.c_int64, C.c_int32,
                                                   _VP, _I64, _D]),
@@ -257,6 +271,13 @@ class Solver:
         """The context's cudaStream_t as an integer handle."""
         return self.L.ib3d_stream(self._h) or 0
 
+    def enable_history(self):
+        self._check(self.L.ib3d_enable_history(self._h), "ib3d_enable_history")
+
+    def attach_net(self, net: "Net | None"):
+        self._check(self.L.ib3d_attach_net(self._h, net._h if net is not None else None), "ib3d_attach_net")
+        self._net = net
+
     def timers_enable(self, on: bool = True):
         self._check(self.L.ib3d_timers_enable(self._h, 1 if on else 0), "ib3d_timers_enable")
 
@@ -304,6 +325,71 @@ class Solver:
         d = st.as_dict()
         d["rc"] = rc
         return d, coef
+
+
+class Net:
+    """The learned warm start's 3-D U-Net (ib3d_net)."""
+
+    def __init__(self, seed: int = 0):
+        self.L = lib()
+        self._h = _VP()
+        rc = self.L.ib3d_net_create(C.byref(self._h), seed)
+        if rc != OK:
+            raise IB3DError(rc, "ib3d_net_create failed")
+        self.nparams = int(self.L.ib3d_net_num_params(self._h))
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            msg = self.L.ib3d_net_last_error(self._h)
+            raise IB3DError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self._h:
+            self.L.ib3d_net_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, np.float32)
+        self._check(self.L.ib3d_net_get_params(self._h, out.ctypes.data_as(_F)), "ib3d_net_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        self._check(self.L.ib3d_net_set_params(self._h, p.ctypes.data_as(_F)), "ib3d_net_set_params")
+
+    def loss_grad(self, x: np.ndarray, target: np.ndarray):
+        """x: [B, S, S, S, 3] (z, y, x, channel), target: [B, S, S, S]."""
+        B, S = x.shape[0], x.shape[1]
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        loss = np.zeros(1)
+        grad = np.zeros(self.nparams, np.float32)
+        out = np.zeros(t.shape, np.float32)
+        self._check(self.L.ib3d_net_loss_grad(self._h, B, S, x.ctypes.data_as(_F), t.ctypes.data_as(_F),
+                                              loss.ctypes.data_as(_D), grad.ctypes.data_as(_F),
+                                              out.ctypes.data_as(_F)), "ib3d_net_loss_grad")
+        return float(loss[0]), grad, out
+
+    def reserve(self, patch: int, capacity: int):
+        self._check(self.L.ib3d_net_dataset_reserve(self._h, patch, capacity), "ib3d_net_dataset_reserve")
+
+    def dataset_size(self) -> int:
+        return int(self.L.ib3d_net_dataset_size(self._h))
+
+    def capture(self, solver: "Solver", npatches: int, seed: int = 0):
+        self._check(self.L.ib3d_net_capture(self._h, solver._h, npatches, seed), "ib3d_net_capture")
+
+    def train(self, steps: int, batch: int = 8, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = np.zeros(1)
+        self._check(self.L.ib3d_net_train(self._h, steps, batch, lr, seed, loss.ctypes.data_as(_D)), "ib3d_net_train")
+        return float(loss[0])
 
 
 def setup_case(cs, params: Params | None = None, **kw) -> Solver:

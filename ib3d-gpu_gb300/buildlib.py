@@ -1,8 +1,9 @@
 """Builds libib3d.so (the CUDA hot path behind include/ib3d.h) in-tree for sm_103a.
 
-Every translation unit is compiled with -fmad=false (no contraction of FP64
-multiply-adds, so the FP64 path keeps the reference's rounding) and the host
-code with -ffp-contract=off. The FP32 inner solve uses explicit fmaf().
+Translation units are compiled with -fmad=false (no contraction of FP64
+multiply-adds, so the FP64 path keeps the reference's rounding), except the
+fast momentum kernel of the mixed-precision path; host code always uses
+-ffp-contract=off. The FP32 inner solve uses explicit fmaf().
 """
 from __future__ import annotations
 
@@ -15,7 +16,9 @@ import subprocess
 HERE = pathlib.Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIB = HERE / "libib3d.so"
-SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu", "noalloc.cu"]
+SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu", "noalloc.cu", "k_momentum_fast.cu", "k_unet.cu", "unet.cu"]
+# translation units whose multiply-adds may contract (results differ from the reference by rounding)
+FMAD_TRUE = {"k_momentum_fast.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,7 +36,10 @@ def flags() -> list[str]:
 
 def _compile(src: str, out_dir: pathlib.Path, extra: list[str]) -> pathlib.Path:
     obj = out_dir / (pathlib.Path(src).stem + ".o")
-    cmd = [nvcc(), *flags(), *extra, "-c", str(CSRC / src), "-o", str(obj)]
+    fl = flags()
+    if src in FMAD_TRUE:
+        fl = [f for f in fl if f != "-fmad=false"] + ["-fmad=true"]
+    cmd = [nvcc(), *fl, *extra, "-c", str(CSRC / src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")

@@ -1,6 +1,7 @@
 // C ABI of the GB300 IB3D hot path (declared in include/ib3d.h): context set-up,
 // host-side grid tables, device residency and the per-step entry points that
 // replace the reference's Fortran subroutine calls.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -153,6 +154,40 @@ void poisson_axis(int n, const std::vector<double>& c, bool dirichlet_hi, std::v
   a[2][n] = 0.0;
 }
 
+// 1-D tables of the fast momentum kernel (k_momentum_fast.cu lists them): the
+// quotients of nsMomentum whose divisors depend only on the grid.
+void fast_tables(const std::vector<double>& d, int n, int axis, const std::vector<double> cc[6][12], int S,
+                 std::vector<double>& out) {
+  auto put = [&](int t, int m, double v) { out[(size_t)(axis * kFastTables + t) * S + m] = std::isfinite(v) ? v : 0.0; };
+  for (int m = 2; m <= n + 1; ++m) {
+    const double dm = d[m], dp = d[m + 1], dl = d[m - 1];
+    put(0, m, dp / (dm + dp));
+    put(1, m, 1.0 / (cc[axis][5][m] * dp));
+    put(2, m, 1.0 / (2.0 * cc[axis][11][m] * dm));
+    put(3, m, 1.0 / (cc[3 + axis][5][m] * (0.5 * (dm + dp))));
+    put(4, m, 1.0 / (2.0 * cc[3 + axis][11][m] * (0.5 * (dm + dl))));
+    const double rn[2] = {dm / dp, (0.5 * (dm + dl)) / (0.5 * (dm + dp))};
+    const double da[2] = {dp, 0.5 * (dm + dp)};
+    for (int f = 0; f < 2; ++f) {
+      const double r = rn[f];
+      const int b = 5 + 8 * f;
+      put(b + 0, m, -1.0 / (r * (r + 1.0)));
+      put(b + 1, m, 1.0 - 1.0 / r);
+      put(b + 2, m, r / (r + 1.0));
+      put(b + 3, m, 2.0 / (r * (r + 1.0)));
+      put(b + 4, m, 2.0 / r);
+      put(b + 5, m, 2.0 / (r + 1.0));
+      put(b + 6, m, 1.0 / da[f]);
+      put(b + 7, m, 1.0 / (2.0 * da[f]));
+    }
+    put(21, m, 2.0 / ((dm + dp) * dp));
+    put(22, m, 2.0 / ((dm + dp) * dm));
+    const double hs = 0.5 * ((dm + dp) + (dm + dl));
+    put(23, m, 2.0 / (hs * (0.5 * (dm + dp))));
+    put(24, m, 2.0 / (hs * (0.5 * (dm + dl))));
+  }
+}
+
 struct Packer {
   std::vector<double> host;
   std::vector<std::pair<const double**, size_t>> fix;
@@ -171,12 +206,20 @@ int alloc_fields(ib3d_ctx* c) {
     if (cudaMemsetAsync(*q, 0, n3 * sizeof(double), c->st) != cudaSuccess) return IB3D_ERR_CUDA;
   }
   if (cudaMalloc(&c->e32, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
-  if (cudaMalloc(&c->e32b, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->r32, n3 * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
+  if (c->d.nx % 2 == 0) {   // colour-packed arrays of the FP32 inner solve (even nx)
+    c->packed_lp = packed_row_length(c->d.nx);
+    const size_t np = (size_t)c->packed_lp * (size_t)c->d.NY2 * (size_t)c->d.NZ2;
+    for (int q = 0; q < 2; ++q) {
+      if (cudaMalloc(&c->ep[q], np * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
+      if (cudaMalloc(&c->rp[q], np * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
+      cudaMemsetAsync(c->ep[q], 0, np * sizeof(float), c->st);
+      cudaMemsetAsync(c->rp[q], 0xff, np * sizeof(float), c->st);   // all-ones bits: NaN
+    }
+  }
   if (cudaMalloc(&c->cell, n3) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->ibmap, n3 * sizeof(int)) != cudaSuccess) return IB3D_ERR_MEMORY;
   cudaMemsetAsync(c->e32, 0, n3 * sizeof(float), c->st);
-  cudaMemsetAsync(c->e32b, 0, n3 * sizeof(float), c->st);
   cudaMemsetAsync(c->r32, 0, n3 * sizeof(float), c->st);
   cudaMemsetAsync(c->cell, 0, n3, c->st);
   cudaMemsetAsync(c->ibmap, 0xff, n3 * sizeof(int), c->st);
@@ -193,8 +236,9 @@ int alloc_fields(ib3d_ctx* c) {
 bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
-         (p->precision == 0 || p->precision == 1) && (p->warm_start == 0 || p->warm_start == 1) &&
-         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1);
+         (p->precision == 0 || p->precision == 1) && (p->warm_start >= 0 && p->warm_start <= 2) &&
+         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
+         (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0));
 }
 
 int fail(ib3d_ctx* c, int code, const char* msg) {
@@ -249,6 +293,7 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
   *out = nullptr;
   if (!valid_params(prm) || nx < 4 || ny < 4 || nz < 4 || !x1n || !y1n || !z1n) return IB3D_ERR_ARG;
   if ((nx + 2) * (ny + 2) * (nz + 2) >= (1ll << 31)) return IB3D_ERR_ARG;
+  if (nz > 65535) return IB3D_ERR_ARG;   // one grid z-index per plane in the FP32 sweep launch
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return IB3D_ERR_CUDA;
   ib3d_ctx* c = new ib3d_ctx();
@@ -335,6 +380,35 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
     if (!rc)
       for (auto& f : fix32) *f.first = c->d_tables32 + f.second;
   }
+  // x coefficients of the colour-packed FP32 sweep, grouped by four cells of one colour
+  if (!rc && nx % 2 == 0) {
+    const int nq = (int)(((nx >> 1) + 3) >> 2);
+    std::vector<float> hp((size_t)2 * 3 * nq * 4, 0.0f);
+    for (int s = 0; s < 2; ++s)
+      for (int q = 0; q < 3; ++q)
+        for (int g = 0; g < nq; ++g)
+          for (int e = 0; e < 4; ++e) {
+            const long long i = 2 + s + 8ll * g + 2 * e;
+            if (i <= nx + 1) hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = (float)c->hac[0][q][i - 1];
+          }
+    if (cudaMalloc(&c->d_axp, hp.size() * sizeof(float)) != cudaSuccess) rc = IB3D_ERR_MEMORY;
+    if (!rc && cudaMemcpy(c->d_axp, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = IB3D_ERR_CUDA;
+    if (!rc)
+      for (int s = 0; s < 2; ++s)
+        for (int q = 0; q < 3; ++q) c->g.axp[s][q] = reinterpret_cast<const float4*>(c->d_axp) + ((size_t)s * 3 + q) * nq;
+  }
+  if (!rc) {
+    const int S = (int)std::max(nx, std::max(ny, nz)) + 3;
+    std::vector<double> ft((size_t)3 * kFastTables * S, 0.0);
+    fast_tables(c->hdx, (int)nx, 0, c->hcc, S, ft);
+    fast_tables(c->hdy, (int)ny, 1, c->hcc, S, ft);
+    fast_tables(c->hdz, (int)nz, 2, c->hcc, S, ft);
+    c->fast_stride = S;
+    if (cudaMalloc(&c->d_fast, ft.size() * sizeof(double)) != cudaSuccess) rc = IB3D_ERR_MEMORY;
+    if (!rc && cudaMemcpy(c->d_fast, ft.data(), ft.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = IB3D_ERR_CUDA;
+  }
   if (!rc) rc = alloc_fields(c);
   if (!rc) rc = ib3d_set_params(c, prm);
   if (!rc && cudaStreamSynchronize(c->st) != cudaSuccess) rc = IB3D_ERR_CUDA;
@@ -352,9 +426,10 @@ void ib3d_destroy(ib3d_ctx* c) {
   timer_fold(c);
   for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
   free_ib(c);
-  void* ptrs[] = {c->d_tables, c->d_tables32, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
-                  c->e32, c->e32b, c->r32, c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
-                  c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan};
+  void* ptrs[] = {c->d_tables, c->d_tables32, c->d_fast, c->d_axp, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
+                  c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
+                  c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
+                  c->hist[0], c->hist[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -527,7 +602,7 @@ int ib3d_timers_read(ib3d_ctx* c, ib3d_timers* out) {
   if (!c || !out) return IB3D_ERR_ARG;
   timer_fold(c);
   IB3D_CUDA(c, cudaStreamSynchronize(c->st));
-  for (int q = 0; q < 9; ++q) out->ms[q] = c->tms[q];
+  for (int q = 0; q < 10; ++q) out->ms[q] = c->tms[q];
   out->sweeps64 = c->t_sweeps64;
   out->sweeps32 = c->t_sweeps32;
   out->outer = c->t_outer;
@@ -544,7 +619,8 @@ int ib3d_synchronize(ib3d_ctx* c) {
 
 int ib3d_ns_momentum(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
-  launch_momentum(c);
+  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c);
+  else launch_momentum(c);
   IB3D_CUDA(c, cudaGetLastError());
   return IB3D_OK;
 }
@@ -575,14 +651,36 @@ int ib3d_pressure_forcing(ib3d_ctx* c) {
   return run_pressure_forcing(c);
 }
 
+int ib3d_enable_history(ib3d_ctx* c) {
+  if (!c) return IB3D_ERR_ARG;
+  for (int q = 0; q < 2; ++q)
+    if (!c->hist[q]) {
+      IB3D_CUDA(c, cudaMalloc(&c->hist[q], (size_t)c->d.n3 * sizeof(double)));
+      IB3D_CUDA(c, cudaMemsetAsync(c->hist[q], 0, (size_t)c->d.n3 * sizeof(double), c->st));
+    }
+  c->hist_valid = 0;
+  return IB3D_OK;
+}
+
 int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
   if (!c) return IB3D_ERR_ARG;
   ib3d_solve_stats st{};
+  if (c->hist[0]) {   // p still holds p^{n-1}: keep it and the one before
+    double* t = c->hist[1];
+    c->hist[1] = c->hist[0];
+    c->hist[0] = t;
+    IB3D_CUDA(c, cudaMemcpyAsync(c->hist[0], c->p, (size_t)c->d.n3 * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    c->hist_valid = std::min(c->hist_valid + 1, 2);
+  }
   unsigned long long* red = reinterpret_cast<unsigned long long*>(c->d_coef + 4);  // divmax, derrStdSt
   IB3D_CUDA(c, cudaMemsetAsync(red, 0, 2 * sizeof(unsigned long long), c->st));
   // divergence writes its max into ctl->aux; copy it aside before the SOR resets ctl
   IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
   launch_divergence(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  if (c->prm.warm_start == IB3D_WARM_LEARNED) {
+    PhaseScope ps(c, PH_NET);
+    net_predict_pc(c);   // until two previous pressures exist, pc keeps the previous step's value
+  }
   IB3D_CUDA(c, cudaMemcpyAsync(red, &c->ctl->aux, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

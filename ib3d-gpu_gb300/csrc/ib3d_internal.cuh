@@ -22,6 +22,7 @@
 namespace ib3d {
 
 constexpr int kBlock = 256;
+constexpr int kFastTables = 25;   // 1-D tables per axis of the fast momentum kernel
 
 // Index helpers: 1-based Fortran (i,j,k) into the padded column-major array.
 struct Dims {
@@ -41,6 +42,10 @@ struct Grid1D {
   // is acx[c][i-1]); [0..2] = columns 1..3.
   const double *acx[3], *acy[3], *acz[3];
   const float *acx32[3], *acy32[3], *acz32[3];
+  // x coefficients regrouped for the colour-packed sweep: axp[s][c][q] holds column c
+  // of Acx at the four cells i = (2+s) + 8q + {0,2,4,6} (s = 0 rows whose colour
+  // starts at i = 2, s = 1 at i = 3), as FP32 float4
+  const float4* axp[2][3];
   // convection tables cc[fam][m], fam 0 uu,1 vv,2 ww,3 uv(=uw),4 vu(=vw),5 wu(=wv)
   const double* cc[6][12];
   // velocity-correction factor deltat/(0.5*(d(i+1)+d(i))) per axis
@@ -79,6 +84,8 @@ struct ForceSched {
 
 }  // namespace ib3d
 
+struct ib3d_net;
+
 struct ib3d_ctx {
   ib3d::Dims d;
   ib3d_params prm;
@@ -94,11 +101,18 @@ struct ib3d_ctx {
 
   // device storage
   double* d_tables = nullptr;  // all 1-D FP64 tables in one allocation
+  double* d_fast = nullptr;    // 3 x kFastTables 1-D tables of the fast momentum kernel
+  int fast_stride = 0;
   float* d_tables32 = nullptr;
+  float* d_axp = nullptr;      // grouped x coefficients of the colour-packed sweep
   ib3d::Grid1D g{};
   double *u = nullptr, *v = nullptr, *w = nullptr, *ut = nullptr, *vt = nullptr, *wt = nullptr;
   double *p = nullptr, *pc = nullptr, *b = nullptr, *bdt = nullptr;
-  float *e32 = nullptr, *e32b = nullptr, *r32 = nullptr;
+  float *e32 = nullptr, *r32 = nullptr;
+  // colour-packed FP32 arrays of the inner solve ([0] red, [1] black); see k_sor32.cu
+  float* ep[2] = {nullptr, nullptr};
+  float* rp[2] = {nullptr, nullptr};
+  int packed_lp = 0;
   unsigned char* cell = nullptr;
   int* ibmap = nullptr;
   ib3d::SolveCtl* ctl = nullptr;
@@ -134,6 +148,11 @@ struct ib3d_ctx {
   long long* d_scan = nullptr;
   size_t scan_cap = 0;
 
+  // previous pressures for the learned warm start: hist[0] = p^{n-1}, hist[1] = p^{n-2}
+  double* hist[2] = {nullptr, nullptr};
+  int hist_valid = 0;
+  ib3d_net* net = nullptr;
+
   // phase timers (ib3d_timers_*) and the launch counter
   bool timing = false;
   struct EvPair {
@@ -142,7 +161,7 @@ struct ib3d_ctx {
   };
   std::vector<EvPair> pending;
   std::vector<cudaEvent_t> pool;
-  double tms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double tms[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   long long t_sweeps64 = 0, t_sweeps32 = 0, t_outer = 0, t_steps = 0;
   long long launches = 0;
 };
@@ -158,10 +177,13 @@ void launch_velocity_bc(ib3d_ctx* c);
 void launch_solid_bc(ib3d_ctx* c);
 void launch_dss_copy(ib3d_ctx* c);
 void launch_initial(ib3d_ctx* c);
-// k_momentum.cu
+// k_momentum.cu, k_momentum_fast.cu
 void launch_momentum(ib3d_ctx* c);
+void launch_momentum_fast(ib3d_ctx* c);
 // k_sor32.cu
-void launch_sor32_fused(ib3d_ctx* c, const float* ein, float* eout, float omega, float om1);
+int packed_row_length(int nx);
+void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1);
+void launch_accumulate_packed(ib3d_ctx* c);
 // k_ib.cu
 int run_surface_norm(ib3d_ctx* c);
 int run_search(ib3d_ctx* c);
@@ -169,12 +191,15 @@ int run_velocity_forcing(ib3d_ctx* c);
 int run_pressure_forcing(ib3d_ctx* c);
 int run_stress(ib3d_ctx* c, int first, double coef[4]);
 
+// unet.cu: pc = the attached network's prediction; nonzero when not available yet
+int net_predict_pc(ib3d_ctx* c);
+
 // error helper: records the message and returns IB3D_ERR_CUDA
 int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where);
 
 // Phase indices of ib3d_timers.ms
 enum Phase { PH_MOMENTUM = 0, PH_BC, PH_FORCING, PH_DIVERGENCE, PH_SOR64, PH_SOR32, PH_RESIDUAL, PH_CORRECT,
-             PH_STRESS };
+             PH_STRESS, PH_NET };
 cudaEvent_t timer_event(ib3d_ctx* c);
 void timer_push(ib3d_ctx* c, int phase, cudaEvent_t a, cudaEvent_t b);
 // Records a start event on construction and an end event on destruction when the
@@ -232,4 +257,13 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* s
   }
 }
 __device__ __forceinline__ double bits_to_double(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// The FP32 SOR update shared by every FP32 sweep kernel: e <- (1-omega) e +
+// omega num / diag, the quotient through the hardware reciprocal (two
+// instructions instead of the IEEE division's sequence). The FP32 sweeps only
+// precondition the FP64 defect correction, whose FP64 residual decides
+// convergence, so the quotient's last-bit rounding does not reach the result.
+__device__ __forceinline__ float sor32_update(float e, float num, float diag, float omega, float om1) {
+  return fmaf(om1, e, __fdividef(omega * num, diag));
+}
 }  // namespace ib3d

@@ -137,8 +137,10 @@ __global__ void __launch_bounds__(kBlock) k_sor64(Dims d, Grid1D g, const double
 __global__ void __launch_bounds__(kBlock) k_residual64(Dims d, Grid1D g, const double* __restrict__ bdt,
                                                        const double* __restrict__ pc,
                                                        const unsigned char* __restrict__ cell,
-                                                       float* __restrict__ r32, SolveCtl* ctl, long long sweep,
-                                                       int decide_mode, double eps, long long max_sweeps) {
+                                                       float* __restrict__ r32, float* __restrict__ rp_red,
+                                                       float* __restrict__ rp_black, int Lp, SolveCtl* ctl,
+                                                       long long sweep, int decide_mode, double eps,
+                                                       long long max_sweeps) {
   if (decide_mode != 2 && ctl->done) return;
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   double m = 0.0;
@@ -158,7 +160,12 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Dims d, Grid1D g, const d
       m = fabs(r);
       rr = (float)r;
     }
-    if (r32) r32[idx] = rr;
+    if (rp_red) {   // colour-packed right-hand side (k_sor32.cu)
+      const long long s = ((long long)(k - 1) * d.NY2 + (j - 1)) * Lp + ((i - 2) >> 1) + 4;
+      (((i + j + k) & 1) ? rp_red : rp_black)[s] = rr;
+    } else if (r32) {
+      r32[idx] = rr;
+    }
   }
   block_max_atomic(m, &ctl->res);
   finish_block(ctl, &ctl->res, decide_mode == 2 ? 0 : decide_mode, sweep, eps, max_sweeps);
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_sor32(Dims d, Grid1D g, const float*
   num = fmaf(-g.acz32[0][k - 1], e[idx - sz], num);
   num = fmaf(-g.acz32[2][k - 1], e[idx + sz], num);
   const float diag = g.acx32[1][i - 1] + g.acy32[1][j - 1] + g.acz32[1][k - 1];
-  e[idx] = fmaf(om1, e[idx], omega * __fdiv_rn(num, diag));
+  e[idx] = sor32_update(e[idx], num, diag, omega, om1);
 }
 
 // pc += e (FP64 accumulation of the FP32 correction), then e = 0.
@@ -397,8 +404,8 @@ int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st) {
       k_sor64<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, P.omega, om1, c->ctl, sweep,
                                              mode_black, P.eps, P.max_sweeps);
       if (resid && (sweep % every) == 0)
-        k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, nullptr, c->ctl,
-                                                            sweep, 0, P.eps, P.max_sweeps);
+        k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, nullptr, nullptr,
+                                                            nullptr, 0, c->ctl, sweep, 0, P.eps, P.max_sweeps);
     }
     }
     IB3D_CUDA(c, cudaGetLastError());
@@ -427,18 +434,21 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   const unsigned ncol = (unsigned)((((long long)d.nx + 1) / 2) * d.ny * d.nz);
   const unsigned gcol = (ncol + kBlock - 1) / kBlock;
   const long long ncell = (long long)d.nx * d.ny * d.nz;
-  const float om = (float)P.omega, om1 = (float)(1.0 - P.omega);
+  const double wi = P.omega_inner > 0.0 ? P.omega_inner : P.omega;
+  const float om = (float)wi, om1 = (float)(1.0 - wi);
   const int inner = P.inner_sweeps < 1 ? 1 : P.inner_sweeps;
+  const bool packed = P.sweep_kernel == 0 && c->ep[0] != nullptr;
   int rc = reset_ctl(c);
   if (rc) return rc;
-  IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
+  if (!packed) IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
   long long sweeps = 0, outer = 0;
   for (;;) {
     {
       PhaseScope ps(c, PH_RESIDUAL);
       c->launches += 1;
-      k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, c->r32, c->ctl, sweeps,
-                                                          0, P.eps, P.max_sweeps);
+      k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, packed ? nullptr : c->r32,
+                                                          packed ? c->rp[0] : nullptr, packed ? c->rp[1] : nullptr,
+                                                          c->packed_lp, c->ctl, sweeps, 0, P.eps, P.max_sweeps);
     }
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);
@@ -446,19 +456,12 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     if (c->h_ctl->done) break;
     {
       PhaseScope ps(c, PH_SOR32);
-      if (P.sweep_kernel == 0) {
-        // one fused launch per sweep, ping-ponging between e32 and e32b
-        c->launches += inner;
-        float* ein = c->e32;
-        float* eout = c->e32b;
-        for (int q = 0; q < inner; ++q) {
-          launch_sor32_fused(c, ein, eout, om, om1);
-          float* t = ein; ein = eout; eout = t;
-        }
-        if (ein != c->e32) { c->e32b = c->e32; c->e32 = ein; }   // c->e32 holds the result
-      } else {
-        c->launches += 2 * inner;
-        for (int q = 0; q < inner; ++q) {
+      c->launches += 2 * inner;
+      for (int q = 0; q < inner; ++q) {
+        if (packed) {
+          launch_sor32_packed(c, 0, om, om1);
+          launch_sor32_packed(c, 1, om, om1);
+        } else {
           k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
           k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
         }
@@ -467,7 +470,8 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     {
       PhaseScope ps(c, PH_RESIDUAL);
       c->launches += 1;
-      k_accumulate<<<nblocks(d.n3), kBlock, 0, c->st>>>(d.n3, c->pc, c->e32);
+      if (packed) launch_accumulate_packed(c);
+      else k_accumulate<<<nblocks(d.n3), kBlock, 0, c->st>>>(d.n3, c->pc, c->e32);
     }
     sweeps += inner;
     ++outer;

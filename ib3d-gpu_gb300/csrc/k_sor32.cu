@@ -1,146 +1,136 @@
-// Fused FP32 red-black SOR sweep: both colours of one sweep in a single pass over
-// memory (the inner solve of the FP64 defect-correction loop).
+// FP32 red-black SOR sweep on colour-packed arrays (the inner solve of the FP64
+// defect-correction loop).
 //
-// A two-kernel sweep (red pass, then black pass) moves each array through the
-// memory system twice per sweep. Here each block owns a 64 x 8 (x,y) tile and a
-// chunk of z planes and marches through z: at plane step kk it computes the new
-// red values of plane kk on the tile plus a one-cell ring, then the new black
-// values of plane kk-1 on the tile (which need the new red values of planes
-// kk-2..kk), and stores plane kk-1. Old values are read from one buffer and new
-// ones written to another, and the red ring is recomputed by every block that needs
-// it, so no block reads another block's results within a sweep: the update is
-// exactly the red-then-black sweep (red reads old black, black reads new red)
-// with the two-kernel form's FP32 operation order, hence the same bits.
+// In the padded Fortran layout a colour pass touches every cache line of e, r and
+// the flags although it updates half the cells. Here each colour lives in its own
+// array: the cells of colour c in row (j,k) are i = i_c + 2m, m = 0..nx/2-1, with
+// i_c = 2 if cell (2,j,k) has colour c, else 3 (red is (i+j+k) odd,
+// subSearch.f90:562). The y and z neighbours of (c, m) are the other colour's
+// entries with the same m in rows j+-1, k+-1; the x neighbours are its entries m-1
+// and m (i_c = 2) or m and m+1 (i_c = 3). Rows carry zero ghost entries on both
+// sides and the arrays carry zero ghost rows, standing in for the grid's ghost
+// layer. Entry m of a row is stored at m + 4 (rows are 16-byte aligned), so a
+// thread updates four consecutive cells of its colour with float4 loads and
+// stores; the x coefficients of those four cells come regrouped as float4 (Grid1D::axp)
+// so that the warp reads them without strided scalar loads. A non-fluid cell carries
+// a NaN right-hand side and keeps its value, 0, so no flag array is read.
 //
-// Non-fluid cells carry a NaN right-hand side (written by the residual kernel), so
-// no flag array is read: a NaN r keeps the cell at its old value, 0.
-//
-// Shared memory per block: four e planes (tile + 2-cell ring), three r planes and
-// three new-red planes (tile + 1-cell ring) = 28.8 KB.
+// Per cell the arithmetic and its order are those of the one-array form (k_sor32
+// in k_pressure.cu), so both give the same bits.
 #include "ib3d_internal.cuh"
 
 namespace ib3d {
 
-namespace {
-constexpr int TX = 64, TY = 8, NT = 256;
-constexpr int EX = TX + 4, EY = TY + 4;   // e tile with a 2-cell ring
-constexpr int RX = TX + 2, RY = TY + 2;   // r / new-red tile with a 1-cell ring
-__device__ __forceinline__ int mod3(int k) { return ((k % 3) + 3) % 3; }
-__device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
-}  // namespace
+// Row length of a packed colour array: the row's cells rounded up to whole float4
+// groups, plus 4 entries of left padding (ghost at 3) and 4 of right padding.
+int packed_row_length(int nx) { return 4 * (((nx >> 1) + 3) >> 2) + 8; }
 
-__global__ void __launch_bounds__(NT) k_sor32_fused(Dims d, Grid1D g, const float* __restrict__ r,
-                                                    const float* __restrict__ ein, float* __restrict__ eout,
-                                                    float omega, float om1, int lz) {
-  __shared__ float se[4][EY][EX];
-  __shared__ float sr[3][RY][RX];
-  __shared__ float sn[3][RY][RX];
-  const int tid = threadIdx.x;
-  const int x0 = 2 + blockIdx.x * TX, y0 = 2 + blockIdx.y * TY;
-  const int k0 = 2 + blockIdx.z * lz, k1 = min(k0 + lz - 1, d.nz + 1);
-
-  auto load_e = [&](int kk) {
-    float(*dst)[EX] = se[kk & 3];
-    const bool plane_ok = kk >= 1 && kk <= d.nz + 2;
-    for (int q = tid; q < EX * EY; q += NT) {
-      const int lx = q % EX - 2, ly = q / EX - 2;
-      const int i = x0 + lx, j = y0 + ly;
-      float v = 0.f;
-      if (plane_ok && i >= 1 && i <= d.nx + 2 && j >= 1 && j <= d.ny + 2) v = ein[d.at(i, j, kk)];
-      dst[ly + 2][lx + 2] = v;
-    }
-  };
-  auto load_r = [&](int kk) {
-    float(*dst)[RX] = sr[mod3(kk)];
-    const bool plane_ok = kk >= 2 && kk <= d.nz + 1;
-    for (int q = tid; q < RX * RY; q += NT) {
-      const int lx = q % RX - 1, ly = q / RX - 1;
-      const int i = x0 + lx, j = y0 + ly;
-      float v = qnan();
-      if (plane_ok && i >= 2 && i <= d.nx + 1 && j >= 2 && j <= d.ny + 1) v = r[d.at(i, j, kk)];
-      dst[ly + 1][lx + 1] = v;
-    }
-  };
-
-  load_e(k0 - 2);
-  load_e(k0 - 1);
-  for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
-    load_e(kk + 1);
-    load_r(kk);
-    __syncthreads();
-    // new red values of plane kk on the tile and its one-cell ring
-    {
-      const float(*em)[EX] = se[(kk - 1) & 3];
-      const float(*e0)[EX] = se[kk & 3];
-      const float(*ep)[EX] = se[(kk + 1) & 3];
-      const float(*rr)[RX] = sr[mod3(kk)];
-      float(*dn)[RX] = sn[mod3(kk)];
-      for (int q = tid; q < (RX / 2) * RY; q += NT) {
-        const int ly = q / (RX / 2) - 1, m = q % (RX / 2);
-        const int j = y0 + ly;
-        const int base = -1 + 2 * m;
-        const int lx = base + ((x0 + base + j + kk + 1) & 1);   // (i+j+kk) odd: red
-        const int i = x0 + lx;
-        const int ex = lx + 2, ey = ly + 2;
-        float val = e0[ey][ex];
-        const float rv = rr[ly + 1][lx + 1];
-        if (rv == rv) {
-          float num = rv;
-          num = fmaf(-g.acx32[0][i - 1], e0[ey][ex - 1], num);
-          num = fmaf(-g.acx32[2][i - 1], e0[ey][ex + 1], num);
-          num = fmaf(-g.acy32[0][j - 1], e0[ey - 1][ex], num);
-          num = fmaf(-g.acy32[2][j - 1], e0[ey + 1][ex], num);
-          num = fmaf(-g.acz32[0][kk - 1], em[ey][ex], num);
-          num = fmaf(-g.acz32[2][kk - 1], ep[ey][ex], num);
-          const float diag = g.acx32[1][i - 1] + g.acy32[1][j - 1] + g.acz32[1][kk - 1];
-          val = fmaf(om1, val, omega * __fdiv_rn(num, diag));
-        }
-        dn[ly + 1][lx + 1] = val;
-      }
-    }
-    __syncthreads();
-    // new black values of plane kk-1 on the tile; store plane kk-1
-    const int km = kk - 1;
-    if (km >= k0) {
-      const int ly = tid >> 5, m = tid & 31;
-      const int j = y0 + ly;
-      const int lxa = 2 * m;
-      const int ia = x0 + lxa;
-      const int lxb = lxa + ((ia + j + km) & 1);    // (i+j+km) even: black
-      const int lxr = 2 * lxa + 1 - lxb;
-      const float(*nm)[RX] = sn[mod3(km - 1)];
-      const float(*n0)[RX] = sn[mod3(km)];
-      const float(*np)[RX] = sn[mod3(km + 1)];
-      const int ib = x0 + lxb;
-      const int bx = lxb + 1, by = ly + 1;
-      float bval = se[km & 3][ly + 2][lxb + 2];
-      const float rv = sr[mod3(km)][by][bx];
-      if (rv == rv) {
-        float num = rv;
-        num = fmaf(-g.acx32[0][ib - 1], n0[by][bx - 1], num);
-        num = fmaf(-g.acx32[2][ib - 1], n0[by][bx + 1], num);
-        num = fmaf(-g.acy32[0][j - 1], n0[by - 1][bx], num);
-        num = fmaf(-g.acy32[2][j - 1], n0[by + 1][bx], num);
-        num = fmaf(-g.acz32[0][km - 1], nm[by][bx], num);
-        num = fmaf(-g.acz32[2][km - 1], np[by][bx], num);
-        const float diag = g.acx32[1][ib - 1] + g.acy32[1][j - 1] + g.acz32[1][km - 1];
-        bval = fmaf(om1, bval, omega * __fdiv_rn(num, diag));
-      }
-      const float rval = n0[by][lxr + 1];
-      if (j <= d.ny + 1) {
-        const int ir = x0 + lxr;
-        if (ib <= d.nx + 1) eout[d.at(ib, j, km)] = bval;
-        if (ir <= d.nx + 1) eout[d.at(ir, j, km)] = rval;
-      }
+// Updates the four cells of one thread. FIRST: the row starts (i = 2) with the
+// colour being updated, so cell c's x neighbours are other-colour entries c-1 and c
+// (else c and c+1) of the row, ox[] holding entries -1..4.
+template <bool FIRST>
+__device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], const float (&ox)[6],
+                                        const float (&sv)[4], const float (&nv)[4], const float (&bv)[4],
+                                        const float (&tv)[4], const float4 a0, const float4 a1, const float4 a2,
+                                        float ay0, float ay1, float ay2, float az0, float az1, float az2,
+                                        float omega, float om1) {
+  const float ax0[4] = {a0.x, a0.y, a0.z, a0.w};
+  const float ax1[4] = {a1.x, a1.y, a1.z, a1.w};
+  const float ax2[4] = {a2.x, a2.y, a2.z, a2.w};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float r = rv[c];
+    if (r == r) {   // fluid cell (NaN marks the others, including the row's padding)
+      const float W = FIRST ? ox[c] : ox[c + 1];
+      const float E = FIRST ? ox[c + 1] : ox[c + 2];
+      float num = r;
+      num = fmaf(-ax0[c], W, num);
+      num = fmaf(-ax2[c], E, num);
+      num = fmaf(-ay0, sv[c], num);
+      num = fmaf(-ay2, nv[c], num);
+      num = fmaf(-az0, bv[c], num);
+      num = fmaf(-az2, tv[c], num);
+      const float diag = ax1[c] + ay1 + az1;
+      ev[c] = sor32_update(ev[c], num, diag, omega, om1);
     }
   }
 }
 
-void launch_sor32_fused(ib3d_ctx* c, const float* ein, float* eout, float omega, float om1) {
+// One colour pass. Block (32, 8): a warp covers 32 float4 groups of one row (j, k),
+// so the row's colour phase is uniform across the warp; grid (ceil(nq/32),
+// ceil(ny/8), nz) maps the rest without integer division.
+template <int COLOR>
+__global__ void __launch_bounds__(256) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
+                                                float* __restrict__ e_own, const float* __restrict__ e_oth,
+                                                int Lp, float omega, float om1) {
+  const int nq = ((d.nx >> 1) + 3) >> 2;
+  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (q >= nq || j > d.ny + 1) return;
+  const long long plane = (long long)(d.ny + 2) * Lp;
+  const long long s0 = (long long)(k - 1) * plane + (long long)(j - 1) * Lp + 4 * q + 4;
+  // does this row start (i = 2) with the colour being updated?
+  const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
+  const float4 rr = *reinterpret_cast<const float4*>(r_own + s0);
+  const float4 eo = *reinterpret_cast<const float4*>(e_own + s0);
+  const float4 ox = *reinterpret_cast<const float4*>(e_oth + s0);
+  const float4 os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
+  const float4 on = *reinterpret_cast<const float4*>(e_oth + s0 + Lp);
+  const float4 ob = *reinterpret_cast<const float4*>(e_oth + s0 - plane);
+  const float4 ot = *reinterpret_cast<const float4*>(e_oth + s0 + plane);
+  const float left = e_oth[s0 - 1], right = e_oth[s0 + 4];
+  const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
+  const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+  const float sv[4] = {os.x, os.y, os.z, os.w};
+  const float nv[4] = {on.x, on.y, on.z, on.w};
+  const float bv[4] = {ob.x, ob.y, ob.z, ob.w};
+  const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
+  float ev[4] = {eo.x, eo.y, eo.z, eo.w};
+  const float ay0 = g.acy32[0][j - 1], ay1 = g.acy32[1][j - 1], ay2 = g.acy32[2][j - 1];
+  const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
+  if (own_first)
+    update4<true>(rv, ev, oxa, sv, nv, bv, tv, g.axp[0][0][q], g.axp[0][1][q], g.axp[0][2][q], ay0, ay1, ay2, az0,
+                  az1, az2, omega, om1);
+  else
+    update4<false>(rv, ev, oxa, sv, nv, bv, tv, g.axp[1][0][q], g.axp[1][1][q], g.axp[1][2][q], ay0, ay1, ay2, az0,
+                   az1, az2, omega, om1);
+  *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+}
+
+// pc += e at every interior cell, reading e from its colour's packed array, then
+// zero e (the next inner solve starts from e = 0).
+__global__ void k_accumulate_packed(Dims d, double* __restrict__ pc, float* __restrict__ e_red,
+                                    float* __restrict__ e_black, int Lp) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) return;
+  const int i = (int)(tid % (unsigned)d.nx) + 2;
+  const unsigned t = tid / (unsigned)d.nx;
+  const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
+  const long long s = ((long long)(k - 1) * (d.ny + 2) + (j - 1)) * Lp + ((i - 2) >> 1) + 4;
+  float* e = ((i + j + k) & 1) ? e_red : e_black;
+  const float x = e[s];
+  if (x != 0.0f) {
+    const long long o = d.at(i, j, k);
+    pc[o] = pc[o] + (double)x;
+    e[s] = 0.0f;
+  }
+}
+
+void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   const Dims& d = c->d;
-  const int lz = 32;
-  dim3 grid((unsigned)((d.nx + TX - 1) / TX), (unsigned)((d.ny + TY - 1) / TY), (unsigned)((d.nz + lz - 1) / lz));
-  k_sor32_fused<<<grid, NT, 0, c->st>>>(d, c->g, c->r32, ein, eout, omega, om1, lz);
+  const int nq = ((d.nx >> 1) + 3) >> 2;
+  const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)d.nz), block(32, 8);
+  if (color == 0)
+    k_sor32p<0><<<grid, block, 0, c->st>>>(d, c->g, c->rp[0], c->ep[0], c->ep[1], c->packed_lp, omega, om1);
+  else
+    k_sor32p<1><<<grid, block, 0, c->st>>>(d, c->g, c->rp[1], c->ep[1], c->ep[0], c->packed_lp, omega, om1);
+}
+
+void launch_accumulate_packed(ib3d_ctx* c) {
+  const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;
+  k_accumulate_packed<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, c->st>>>(c->d, c->pc, c->ep[0], c->ep[1],
+                                                                                   c->packed_lp);
 }
 
 }  // namespace ib3d

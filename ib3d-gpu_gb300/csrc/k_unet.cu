@@ -1,0 +1,407 @@
+// Kernels of the learned warm start: a small 3-D U-Net in BF16 with FP32
+// accumulation (forward, backward, Adam). Host orchestration is in unet.cu.
+//
+// Activations are channels-last BF16 tensors [voxel][channel] over B x D x H x W
+// voxels; a tensor can be a channel slice of a wider buffer (channel stride cs,
+// offset co), which is how the U-Net's skip concatenations are stored. Channel
+// counts are multiples of 16.
+//
+// 3x3x3 convolutions (zero padding) are implicit GEMMs on the BF16 tensor cores
+// (mma.sync m16n8k16, FP32 accumulators): rows are voxels, columns are output
+// channels, and the reduction runs over 27 taps x input channels, gathering each
+// A fragment straight from the channels-last activations (two consecutive
+// channels per 32-bit load). The same kernel computes the input gradient with
+// mirrored taps and transposed weights. Weight gradients are reduced on the CUDA
+// cores in FP32.
+#include <cuda_bf16.h>
+
+#include "ib3d_internal.cuh"
+#include "unet.cuh"
+
+namespace ib3d {
+namespace unet {
+
+namespace {
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void decode(long long m, const Vol& v, int& b, int& z, int& y, int& x) {
+  x = (int)(m % v.W);
+  long long t = m / v.W;
+  y = (int)(t % v.H);
+  t /= v.H;
+  z = (int)(t % v.D);
+  b = (int)(t / v.D);
+}
+
+}  // namespace
+
+// Y[v][n] = act( sum_{tap,k} X[v + sign*off(tap)][k] * Wt[n][tap][k] + bias[n] ).
+// One warp computes 32 voxels x (8*NT) channels.
+template <int NT>
+__global__ void __launch_bounds__(128) k_conv3(Vol vol, Act X, int K, const bf16* __restrict__ Wt,
+                                               const float* __restrict__ bias, int relu, int sign, Act Y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t4 = lane & 3;
+  const long long M = vol.voxels();
+  const long long m0 = ((long long)blockIdx.x * 4 + warp) * 32;
+  if (m0 >= M) return;
+  int vb[4], vz[4], vy[4], vx[4];
+  bool vok[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const long long m = m0 + g + 8 * r;
+    vok[r] = m < M;
+    decode(vok[r] ? m : 0, vol, vb[r], vz[r], vy[r], vx[r]);
+  }
+  float acc[2][NT][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
+  for (int tap = 0; tap < 27; ++tap) {
+    const int dz = sign * (tap / 9 - 1), dy = sign * ((tap / 3) % 3 - 1), dx = sign * (tap % 3 - 1);
+    const bf16* src[4];
+    bool ok[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int z = vz[r] + dz, y = vy[r] + dy, x = vx[r] + dx;
+      ok[r] = vok[r] && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W;
+      const long long sv = (((long long)vb[r] * vol.D + (ok[r] ? z : 0)) * vol.H + (ok[r] ? y : 0)) * vol.W +
+                           (ok[r] ? x : 0);
+      src[r] = X.p + sv * X.cs + X.co + 2 * t4;
+    }
+    const bf16* wbase = Wt + (size_t)tap * K + 2 * t4;
+    for (int kc = 0; kc < K; kc += 16) {
+      uint32_t a[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const int r0 = 2 * mt, r1 = 2 * mt + 1;
+        a[mt][0] = ok[r0] ? ld_pair(src[r0] + kc) : 0u;
+        a[mt][1] = ok[r1] ? ld_pair(src[r1] + kc) : 0u;
+        a[mt][2] = ok[r0] ? ld_pair(src[r0] + kc + 8) : 0u;
+        a[mt][3] = ok[r1] ? ld_pair(src[r1] + kc + 8) : 0u;
+      }
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const bf16* wp = wbase + (size_t)(nt * 8 + g) * 27 * K + kc;
+        const uint32_t b0 = ld_pair(wp), b1 = ld_pair(wp + 8);
+        mma_bf16(acc[0][nt], a[0], b0, b1);
+        mma_bf16(acc[1][nt], a[1], b0, b1);
+      }
+    }
+  }
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = 2 * mt + h;
+      if (!vok[r]) continue;
+      const long long m = m0 + g + 8 * r;
+      bf16* dst = Y.p + m * Y.cs + Y.co;
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int n = nt * 8 + 2 * t4;
+        float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
+        if (bias) { v0 += bias[n]; v1 += bias[n + 1]; }
+        if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+        *reinterpret_cast<__nv_bfloat162*>(dst + n) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+}
+
+// dW[n][tap][k] += sum_v dZ[v][n] * X[v + off(tap)][k]   (FP32, CUDA cores)
+// grid: (voxel chunks, 27 taps); each block reduces kWgTile voxels at a time through
+// shared memory and adds its partial sums to dW with atomics.
+constexpr int kWgTile = 32;
+__global__ void __launch_bounds__(256) k_wgrad(Vol vol, Act dZ, int N, Act X, int K, float* __restrict__ dW,
+                                               long long chunk) {
+  extern __shared__ float sm[];
+  float* sZ = sm;                    // [kWgTile][N]
+  float* sX = sm + kWgTile * N;      // [kWgTile][K]
+  const int tap = blockIdx.y;
+  const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  const long long M = vol.voxels();
+  const long long v0 = (long long)blockIdx.x * chunk, v1 = min(M, v0 + chunk);
+  const int NK = N * K;
+  float acc[24];
+#pragma unroll
+  for (int q = 0; q < 24; ++q) acc[q] = 0.f;
+  for (long long vt = v0; vt < v1; vt += kWgTile) {
+    for (int e = threadIdx.x; e < kWgTile * N; e += blockDim.x) {
+      const int lv = e / N, n = e % N;
+      const long long m = vt + lv;
+      sZ[e] = m < v1 ? __bfloat162float(dZ.p[m * dZ.cs + dZ.co + n]) : 0.f;
+    }
+    for (int e = threadIdx.x; e < kWgTile * K; e += blockDim.x) {
+      const int lv = e / K, k = e % K;
+      const long long m = vt + lv;
+      float val = 0.f;
+      if (m < v1) {
+        int b, z, y, x;
+        decode(m, vol, b, z, y, x);
+        z += dz; y += dy; x += dx;
+        if (z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W) {
+          const long long sv = (((long long)b * vol.D + z) * vol.H + y) * vol.W + x;
+          val = __bfloat162float(X.p[sv * X.cs + X.co + k]);
+        }
+      }
+      sX[e] = val;
+    }
+    __syncthreads();
+    for (int q = 0; q < 24; ++q) {
+      const int pidx = threadIdx.x + q * 256;
+      if (pidx >= NK) break;
+      const int n = pidx / K, k = pidx % K;
+      float s = acc[q];
+#pragma unroll 8
+      for (int lv = 0; lv < kWgTile; ++lv) s = fmaf(sZ[lv * N + n], sX[lv * K + k], s);
+      acc[q] = s;
+    }
+    __syncthreads();
+  }
+  for (int q = 0; q < 24; ++q) {
+    const int pidx = threadIdx.x + q * 256;
+    if (pidx >= NK) break;
+    const int n = pidx / K, k = pidx % K;
+    atomicAdd(&dW[((size_t)n * 27 + tap) * K + k], acc[q]);
+  }
+}
+
+// db[n] += sum_v dZ[v][n]
+__global__ void k_bias_grad(long long M, Act dZ, int N, float* __restrict__ db) {
+  __shared__ float s[64];
+  if (threadIdx.x < N) s[threadIdx.x] = 0.f;
+  __syncthreads();
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const int n = threadIdx.x % N, lane_group = threadIdx.x / N, groups = blockDim.x / N;
+  for (long long m = (long long)blockIdx.x * groups + lane_group; m < M; m += (long long)gridDim.x * groups)
+    acc[0] += __bfloat162float(dZ.p[m * dZ.cs + dZ.co + n]);
+  if (lane_group < groups) atomicAdd(&s[n], acc[0]);
+  __syncthreads();
+  if (threadIdx.x < N) atomicAdd(&db[threadIdx.x], s[threadIdx.x]);
+}
+
+// dY *= (Y > 0): ReLU backward through the layer's own output, in place.
+__global__ void k_relu_bwd(long long M, int C, Act dY, Act Y) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M * C) return;
+  const long long m = e / C;
+  const int c = (int)(e % C);
+  if (!(__bfloat162float(Y.p[m * Y.cs + Y.co + c]) > 0.f)) dY.p[m * dY.cs + dY.co + c] = __float2bfloat16(0.f);
+}
+
+// 2x2x2 average pooling: out has half the extent of in along each axis.
+__global__ void k_pool_fwd(Vol out, int C, Act in, Act o) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= out.voxels() * C) return;
+  const long long m = e / C;
+  const int c = (int)(e % C);
+  int b, z, y, x;
+  decode(m, out, b, z, y, x);
+  const int D2 = out.D * 2, H2 = out.H * 2, W2 = out.W * 2;
+  float s = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const long long sv = (((long long)b * D2 + 2 * z + (q >> 2)) * H2 + 2 * y + ((q >> 1) & 1)) * W2 + 2 * x + (q & 1);
+    s += __bfloat162float(in.p[sv * in.cs + in.co + c]);
+  }
+  o.p[m * o.cs + o.co + c] = __float2bfloat16(0.125f * s);
+}
+
+// gin[child] (+)= gout[parent] / 8
+__global__ void k_pool_bwd(Vol out, int C, Act gout, Act gin, int accumulate) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= out.voxels() * C) return;
+  const long long m = e / C;
+  const int c = (int)(e % C);
+  int b, z, y, x;
+  decode(m, out, b, z, y, x);
+  const int D2 = out.D * 2, H2 = out.H * 2, W2 = out.W * 2;
+  const float g = 0.125f * __bfloat162float(gout.p[m * gout.cs + gout.co + c]);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const long long sv = (((long long)b * D2 + 2 * z + (q >> 2)) * H2 + 2 * y + ((q >> 1) & 1)) * W2 + 2 * x + (q & 1);
+    bf16* d = gin.p + sv * gin.cs + gin.co + c;
+    *d = __float2bfloat16(accumulate ? __bfloat162float(*d) + g : g);
+  }
+}
+
+// nearest-neighbour upsampling x2: fine voxel takes its parent's value.
+__global__ void k_up_fwd(Vol fine, int C, Act in, Act o) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= fine.voxels() * C) return;
+  const long long m = e / C;
+  const int c = (int)(e % C);
+  int b, z, y, x;
+  decode(m, fine, b, z, y, x);
+  const long long pv = (((long long)b * (fine.D / 2) + z / 2) * (fine.H / 2) + y / 2) * (fine.W / 2) + x / 2;
+  o.p[m * o.cs + o.co + c] = in.p[pv * in.cs + in.co + c];
+}
+
+// parent gradient = sum of its eight children's gradients.
+__global__ void k_up_bwd(Vol coarse, int C, Act gfine, Act gout) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= coarse.voxels() * C) return;
+  const long long m = e / C;
+  const int c = (int)(e % C);
+  int b, z, y, x;
+  decode(m, coarse, b, z, y, x);
+  const int D2 = coarse.D * 2, H2 = coarse.H * 2, W2 = coarse.W * 2;
+  float s = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const long long sv = (((long long)b * D2 + 2 * z + (q >> 2)) * H2 + 2 * y + ((q >> 1) & 1)) * W2 + 2 * x + (q & 1);
+    s += __bfloat162float(gfine.p[sv * gfine.cs + gfine.co + c]);
+  }
+  gout.p[m * gout.cs + gout.co + c] = __float2bfloat16(s);
+}
+
+// 1x1 head: out[v] = sum_c w[c] * in[v][c] + b   (FP32 output)
+__global__ void k_head_fwd(long long M, int C, Act in, const float* __restrict__ w, float* __restrict__ out) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  float s = w[C];
+  for (int c = 0; c < C; ++c) s = fmaf(w[c], __bfloat162float(in.p[m * in.cs + in.co + c]), s);
+  out[m] = s;
+}
+
+// gin[v][c] = gout[v] * w[c]; dw[c] += sum_v gout[v] * in[v][c]; dw[C] += sum_v gout[v]
+__global__ void k_head_bwd(long long M, int C, Act in, const float* __restrict__ w, const float* __restrict__ gout,
+                           Act gin, float* __restrict__ dw) {
+  __shared__ float s[33];
+  if (threadIdx.x <= C) s[threadIdx.x] = 0.f;
+  __syncthreads();
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < M) {
+    const float g = gout[m];
+    for (int c = 0; c < C; ++c) {
+      gin.p[m * gin.cs + gin.co + c] = __float2bfloat16(g * w[c]);
+      atomicAdd(&s[c], g * __bfloat162float(in.p[m * in.cs + in.co + c]));
+    }
+    atomicAdd(&s[C], g);
+  }
+  __syncthreads();
+  if (threadIdx.x <= C) atomicAdd(&dw[threadIdx.x], s[threadIdx.x]);
+}
+
+// mean squared error: g = 2 (out - t) / M, loss += sum (out - t)^2 / M
+__global__ void k_mse(long long M, const float* __restrict__ out, const float* __restrict__ t, float* __restrict__ g,
+                      double* loss) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float d = 0.f;
+  if (m < M) {
+    d = out[m] - t[m];
+    g[m] = 2.f * d / (float)M;
+  }
+  float s = d * d;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s != 0.f) atomicAdd(loss, (double)s / (double)M);
+}
+
+// Adam (FP32 master weights) and the BF16 copies the kernels read: the forward
+// layout [n][tap][k] and the transposed input-gradient layout [k][tap][n].
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, float lr, float b1, float b2, float c1, float c2, float eps) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float gg = g[e];
+  const float a = b1 * m1[e] + (1.f - b1) * gg;
+  const float b = b2 * m2[e] + (1.f - b2) * gg * gg;
+  m1[e] = a;
+  m2[e] = b;
+  p[e] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+__global__ void k_cast_conv_weights(int N, int K, const float* __restrict__ w, bf16* __restrict__ wf,
+                                    bf16* __restrict__ wt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= N * 27 * K) return;
+  const int k = e % K, tap = (e / K) % 27, n = e / (27 * K);
+  const bf16 v = __float2bfloat16(w[e]);
+  wf[e] = v;
+  wt[((size_t)k * 27 + tap) * N + n] = v;
+}
+
+// ------------------------------------------------------------ launch helpers
+
+void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const float* bias, int relu, int sign, Act Y,
+          int N) {
+  const long long M = vol.voxels();
+  const unsigned nb = (unsigned)((M + 127) / 128);
+  switch (N) {
+    case 16: k_conv3<2><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    case 32: k_conv3<4><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    case 48: k_conv3<6><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    case 64: k_conv3<8><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    case 96: k_conv3<12><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    default: break;
+  }
+}
+
+void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW) {
+  const long long M = vol.voxels();
+  const long long chunk = 4096;
+  dim3 grid((unsigned)((M + chunk - 1) / chunk), 27);
+  const size_t smem = (size_t)kWgTile * (N + K) * sizeof(float);
+  k_wgrad<<<grid, 256, smem, st>>>(vol, dZ, N, X, K, dW, chunk);
+}
+
+void bias_grad(cudaStream_t st, long long M, Act dZ, int N, float* db) {
+  k_bias_grad<<<256, 256, 0, st>>>(M, dZ, N, db);
+}
+
+void relu_bwd(cudaStream_t st, long long M, int C, Act dY, Act Y) {
+  k_relu_bwd<<<(unsigned)((M * C + 255) / 256), 256, 0, st>>>(M, C, dY, Y);
+}
+
+void pool_fwd(cudaStream_t st, const Vol& out, int C, Act in, Act o) {
+  k_pool_fwd<<<(unsigned)((out.voxels() * C + 255) / 256), 256, 0, st>>>(out, C, in, o);
+}
+
+void pool_bwd(cudaStream_t st, const Vol& out, int C, Act gout, Act gin, int accumulate) {
+  k_pool_bwd<<<(unsigned)((out.voxels() * C + 255) / 256), 256, 0, st>>>(out, C, gout, gin, accumulate);
+}
+
+void up_fwd(cudaStream_t st, const Vol& fine, int C, Act in, Act o) {
+  k_up_fwd<<<(unsigned)((fine.voxels() * C + 255) / 256), 256, 0, st>>>(fine, C, in, o);
+}
+
+void up_bwd(cudaStream_t st, const Vol& coarse, int C, Act gfine, Act gout) {
+  k_up_bwd<<<(unsigned)((coarse.voxels() * C + 255) / 256), 256, 0, st>>>(coarse, C, gfine, gout);
+}
+
+void head_fwd(cudaStream_t st, long long M, int C, Act in, const float* w, float* out) {
+  k_head_fwd<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, C, in, w, out);
+}
+
+void head_bwd(cudaStream_t st, long long M, int C, Act in, const float* w, const float* gout, Act gin, float* dw) {
+  k_head_bwd<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, C, in, w, gout, gin, dw);
+}
+
+void mse(cudaStream_t st, long long M, const float* out, const float* t, float* g, double* loss) {
+  k_mse<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(M, out, t, g, loss);
+}
+
+void adam(cudaStream_t st, int n, float* p, const float* g, float* m1, float* m2, float lr, int step) {
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<(n + 255) / 256, 256, 0, st>>>(n, p, g, m1, m2, lr, b1, b2, c1, c2, 1e-8f);
+}
+
+void cast_conv_weights(cudaStream_t st, int N, int K, const float* w, bf16* wf, bf16* wt) {
+  k_cast_conv_weights<<<(N * 27 * K + 255) / 256, 256, 0, st>>>(N, K, w, wf, wt);
+}
+
+}  // namespace unet
+}  // namespace ib3d

@@ -136,7 +136,7 @@ __global__ void k_na_sor32(Dims d, Coefs A, const float* __restrict__ r32, float
   num = fmaf(-(float)A.z(0, k - 1), e[idx - sz], num);
   num = fmaf(-(float)A.z(2, k - 1), e[idx + sz], num);
   const float diag = (float)A.x(1, i - 1) + (float)A.y(1, j - 1) + (float)A.z(1, k - 1);
-  e[idx] = fmaf(om1, e[idx], omega * __fdiv_rn(num, diag));
+  e[idx] = sor32_update(e[idx], num, diag, omega, om1);
 }
 
 __global__ void k_na_accumulate(long long n3, double* __restrict__ pc, float* __restrict__ e) {

@@ -1,0 +1,520 @@
+// Learned warm start of the pressure solve: a 3-level 3-D U-Net (16/32/64
+// channels, 3x3x3 convolutions, 2x2x2 average pooling, nearest upsampling, skip
+// concatenations, 1x1 head; 0.36 M parameters) in BF16 with FP32 accumulation,
+// trained with Adam on snapshots the solver generates.
+//
+// Inputs per cell: (p^{n-1} - p^{n-2})/s1, (b/dt)^n/s2, p^{n-1}/s3 with s1, s2, s3
+// the RMS of each over the fluid cells (the difference is taken in FP64 before the
+// cast to BF16, which would otherwise erase it). Output: the pressure correction
+// pc^n/s1, used as the SOR initial guess; the FP64 defect-correction loop still
+// stops at the same FP64 residual, so a poor guess only costs sweeps.
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "ib3d_internal.cuh"
+#include "unet.cuh"
+
+using namespace ib3d;
+using namespace ib3d::unet;
+
+namespace {
+
+struct Layer {
+  int N, K, Kreal;
+  size_t w, b;   // offsets of the FP32 weights [N][27][K] and biases [N] in the parameter vector
+};
+// conv1a conv1b | conv2a conv2b | conv3a conv3b | conv4a conv4b | conv5a conv5b
+constexpr int kL = 10;
+const int kN[kL] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16};
+const int kK[kL] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16};
+const int kKreal[kL] = {3, 16, 16, 32, 32, 64, 96, 32, 48, 16};
+
+struct Buffers {
+  Vol v1{}, v2{}, v3{};
+  bool grads = false;
+  std::vector<void*> owned;
+  // level 1
+  bf16 *in0, *a1, *cat5, *a5, *d1;
+  float *out, *gout, *tgt;
+  bf16 *g_a1, *g_cat5, *g_a5, *g_d1;
+  // level 2
+  bf16 *p1, *a2, *cat4, *a4, *d2;
+  bf16 *g_p1, *g_a2, *g_cat4, *g_a4, *g_d2;
+  // level 3
+  bf16 *p2, *a3, *b;
+  bf16 *g_p2, *g_a3, *g_b;
+};
+
+}  // namespace
+
+struct ib3d_net {
+  cudaStream_t st = nullptr;
+  std::string err;
+  Layer L[kL];
+  size_t head = 0;     // offset of the head weights (16) and bias (1)
+  size_t nparam = 0;
+  float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
+  bf16 *wf = nullptr, *wt = nullptr;   // BF16 copies: forward [N][27][K], transposed [K][27][N]
+  int step = 0;
+  Buffers buf;
+  // training set
+  int S = 0;
+  long long cap = 0, count = 0;
+  bf16* ds_in = nullptr;   // [patch][S^3][4]
+  float* ds_t = nullptr;   // [patch][S^3]
+  double* d_loss = nullptr;
+  double* d_red = nullptr; // reductions for normalisation
+};
+
+namespace {
+
+int fail(ib3d_net* n, int code, const char* msg) {
+  if (n) n->err = msg;
+  return code;
+}
+#define NET_CUDA(n, expr)                                                              \
+  do {                                                                                 \
+    cudaError_t _e = (expr);                                                           \
+    if (_e != cudaSuccess) return fail((n), IB3D_ERR_CUDA, cudaGetErrorString(_e));    \
+  } while (0)
+
+void free_buffers(Buffers& b) {
+  for (void* q : b.owned) cudaFree(q);
+  b = Buffers{};
+}
+
+// Activation (and, for training, gradient) buffers for one input volume.
+int ensure_buffers(ib3d_net* n, const Vol& v1, bool grads) {
+  Buffers& b = n->buf;
+  if (b.v1.B == v1.B && b.v1.D == v1.D && b.v1.H == v1.H && b.v1.W == v1.W && (b.grads || !grads)) return IB3D_OK;
+  free_buffers(b);
+  b.v1 = v1;
+  b.v2 = {v1.B, v1.D / 2, v1.H / 2, v1.W / 2};
+  b.v3 = {v1.B, v1.D / 4, v1.H / 4, v1.W / 4};
+  b.grads = grads;
+  const long long m1 = b.v1.voxels(), m2 = b.v2.voxels(), m3 = b.v3.voxels();
+  auto alloc_bf = [&](bf16** q, long long vox, int c) -> bool {
+    if (cudaMalloc(q, (size_t)vox * c * sizeof(bf16)) != cudaSuccess) return false;
+    cudaMemsetAsync(*q, 0, (size_t)vox * c * sizeof(bf16), n->st);
+    b.owned.push_back(*q);
+    return true;
+  };
+  auto alloc_f = [&](float** q, long long vox) -> bool {
+    if (cudaMalloc(q, (size_t)vox * sizeof(float)) != cudaSuccess) return false;
+    b.owned.push_back(*q);
+    return true;
+  };
+  bool ok = alloc_bf(&b.in0, m1, 16) && alloc_bf(&b.a1, m1, 16) && alloc_bf(&b.cat5, m1, 48) &&
+            alloc_bf(&b.a5, m1, 16) && alloc_bf(&b.d1, m1, 16) && alloc_f(&b.out, m1) && alloc_bf(&b.p1, m2, 16) &&
+            alloc_bf(&b.a2, m2, 32) && alloc_bf(&b.cat4, m2, 96) && alloc_bf(&b.a4, m2, 32) &&
+            alloc_bf(&b.d2, m2, 32) && alloc_bf(&b.p2, m3, 32) && alloc_bf(&b.a3, m3, 64) && alloc_bf(&b.b, m3, 64);
+  if (ok && grads)
+    ok = alloc_f(&b.gout, m1) && alloc_f(&b.tgt, m1) && alloc_bf(&b.g_a1, m1, 16) && alloc_bf(&b.g_cat5, m1, 48) &&
+         alloc_bf(&b.g_a5, m1, 16) && alloc_bf(&b.g_d1, m1, 16) && alloc_bf(&b.g_p1, m2, 16) &&
+         alloc_bf(&b.g_a2, m2, 32) && alloc_bf(&b.g_cat4, m2, 96) && alloc_bf(&b.g_a4, m2, 32) &&
+         alloc_bf(&b.g_d2, m2, 32) && alloc_bf(&b.g_p2, m3, 32) && alloc_bf(&b.g_a3, m3, 64) &&
+         alloc_bf(&b.g_b, m3, 64);
+  if (!ok) {
+    free_buffers(b);
+    return fail(n, IB3D_ERR_MEMORY, "ib3d_net: activation buffers");
+  }
+  return IB3D_OK;
+}
+
+Act A(bf16* p, int cs, int co = 0) { return Act{p, cs, co}; }
+
+const bf16* wf(ib3d_net* n, int l) { return n->wf + n->L[l].w; }
+const bf16* wt(ib3d_net* n, int l) { return n->wt + n->L[l].w; }
+const float* bias(ib3d_net* n, int l) { return n->p + n->L[l].b; }
+
+void forward(ib3d_net* n) {
+  Buffers& b = n->buf;
+  cudaStream_t st = n->st;
+  conv(st, b.v1, A(b.in0, 16), 16, wf(n, 0), bias(n, 0), 1, 1, A(b.a1, 16), 16);
+  conv(st, b.v1, A(b.a1, 16), 16, wf(n, 1), bias(n, 1), 1, 1, A(b.cat5, 48, 32), 16);   // e1
+  pool_fwd(st, b.v2, 16, A(b.cat5, 48, 32), A(b.p1, 16));
+  conv(st, b.v2, A(b.p1, 16), 16, wf(n, 2), bias(n, 2), 1, 1, A(b.a2, 32), 32);
+  conv(st, b.v2, A(b.a2, 32), 32, wf(n, 3), bias(n, 3), 1, 1, A(b.cat4, 96, 64), 32);   // e2
+  pool_fwd(st, b.v3, 32, A(b.cat4, 96, 64), A(b.p2, 32));
+  conv(st, b.v3, A(b.p2, 32), 32, wf(n, 4), bias(n, 4), 1, 1, A(b.a3, 64), 64);
+  conv(st, b.v3, A(b.a3, 64), 64, wf(n, 5), bias(n, 5), 1, 1, A(b.b, 64), 64);
+  up_fwd(st, b.v2, 64, A(b.b, 64), A(b.cat4, 96, 0));
+  conv(st, b.v2, A(b.cat4, 96), 96, wf(n, 6), bias(n, 6), 1, 1, A(b.a4, 32), 32);
+  conv(st, b.v2, A(b.a4, 32), 32, wf(n, 7), bias(n, 7), 1, 1, A(b.d2, 32), 32);
+  up_fwd(st, b.v1, 32, A(b.d2, 32), A(b.cat5, 48, 0));
+  conv(st, b.v1, A(b.cat5, 48), 48, wf(n, 8), bias(n, 8), 1, 1, A(b.a5, 16), 16);
+  conv(st, b.v1, A(b.a5, 16), 16, wf(n, 9), bias(n, 9), 1, 1, A(b.d1, 16), 16);
+  head_fwd(st, b.v1.voxels(), 16, A(b.d1, 16), n->p + n->head, b.out);
+}
+
+// Backward of conv layer l with output Y (gradient gY, overwritten by the ReLU
+// mask) and input X; writes the input gradient to gX unless gX.p is null.
+void conv_bwd(ib3d_net* n, int l, const Vol& v, Act X, Act Y, Act gY, Act gX) {
+  const Layer& ly = n->L[l];
+  const long long M = v.voxels();
+  relu_bwd(n->st, M, ly.N, gY, Y);
+  bias_grad(n->st, M, gY, ly.N, n->g + ly.b);
+  wgrad(n->st, v, gY, ly.N, X, ly.K, n->g + ly.w);
+  if (gX.p) conv(n->st, v, gY, ly.N, wt(n, l), nullptr, 0, -1, gX, ly.K);
+}
+
+void backward(ib3d_net* n) {
+  Buffers& b = n->buf;
+  cudaStream_t st = n->st;
+  head_bwd(st, b.v1.voxels(), 16, A(b.d1, 16), n->p + n->head, b.gout, A(b.g_d1, 16), n->g + n->head);
+  conv_bwd(n, 9, b.v1, A(b.a5, 16), A(b.d1, 16), A(b.g_d1, 16), A(b.g_a5, 16));
+  conv_bwd(n, 8, b.v1, A(b.cat5, 48), A(b.a5, 16), A(b.g_a5, 16), A(b.g_cat5, 48));
+  up_bwd(st, b.v2, 32, A(b.g_cat5, 48, 0), A(b.g_d2, 32));
+  conv_bwd(n, 7, b.v2, A(b.a4, 32), A(b.d2, 32), A(b.g_d2, 32), A(b.g_a4, 32));
+  conv_bwd(n, 6, b.v2, A(b.cat4, 96), A(b.a4, 32), A(b.g_a4, 32), A(b.g_cat4, 96));
+  up_bwd(st, b.v3, 64, A(b.g_cat4, 96, 0), A(b.g_b, 64));
+  conv_bwd(n, 5, b.v3, A(b.a3, 64), A(b.b, 64), A(b.g_b, 64), A(b.g_a3, 64));
+  conv_bwd(n, 4, b.v3, A(b.p2, 32), A(b.a3, 64), A(b.g_a3, 64), A(b.g_p2, 32));
+  pool_bwd(st, b.v3, 32, A(b.g_p2, 32), A(b.g_cat4, 96, 64), 1);
+  conv_bwd(n, 3, b.v2, A(b.a2, 32), A(b.cat4, 96, 64), A(b.g_cat4, 96, 64), A(b.g_a2, 32));
+  conv_bwd(n, 2, b.v2, A(b.p1, 16), A(b.a2, 32), A(b.g_a2, 32), A(b.g_p1, 16));
+  pool_bwd(st, b.v2, 16, A(b.g_p1, 16), A(b.g_cat5, 48, 32), 1);
+  conv_bwd(n, 1, b.v1, A(b.a1, 16), A(b.cat5, 48, 32), A(b.g_cat5, 48, 32), A(b.g_a1, 16));
+  conv_bwd(n, 0, b.v1, A(b.in0, 16), A(b.a1, 16), A(b.g_a1, 16), Act{nullptr, 0, 0});
+}
+
+void cast_weights(ib3d_net* n) {
+  for (int l = 0; l < kL; ++l) cast_conv_weights(n->st, n->L[l].N, n->L[l].K, n->p + n->L[l].w, n->wf + n->L[l].w,
+                                                   n->wt + n->L[l].w);
+}
+
+// ------------------------------------------------------------- data kernels
+
+// RMS inputs over fluid cells: sums of (h1-h2)^2, (b/dt)^2, h1^2 and the fluid count.
+__global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, const double* __restrict__ h1,
+                            const double* __restrict__ h2, const double* __restrict__ bdt, double* sums) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double s[4] = {0, 0, 0, 0};
+  if (tid < (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) {
+    const int i = (int)(tid % (unsigned)d.nx) + 2;
+    const unsigned t = tid / (unsigned)d.nx;
+    const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
+    const long long o = d.at(i, j, k);
+    if (cell[o] == 0) {
+      const double dp = h1[o] - h2[o];
+      s[0] = dp * dp; s[1] = bdt[o] * bdt[o]; s[2] = h1[o] * h1[o]; s[3] = 1.0;
+    }
+  }
+  for (int q = 0; q < 4; ++q) {
+    double x = s[q];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31) == 0 && x != 0.0) atomicAdd(&sums[q], x);
+  }
+}
+
+struct Norm {
+  double s1, s2, s3;
+};
+
+// Input channels of one cell (see the file header); channels 3..15 are zero.
+__device__ __forceinline__ void cell_inputs(const Dims& d, long long o, const double* h1, const double* h2,
+                                            const double* bdt, Norm nm, float in[3]) {
+  in[0] = (float)((h1[o] - h2[o]) / nm.s1);
+  in[1] = (float)(bdt[o] / nm.s2);
+  in[2] = (float)(h1[o] / nm.s3);
+}
+
+// Full-domain input volume (1 x D x H x W with the interior at the origin, padded
+// with zeros to multiples of 4).
+__global__ void k_pack_domain(Dims d, Vol v, const double* __restrict__ h1, const double* __restrict__ h2,
+                              const double* __restrict__ bdt, Norm nm, bf16* __restrict__ in0) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= v.voxels()) return;
+  const int x = (int)(m % v.W), y = (int)((m / v.W) % v.H), z = (int)(m / ((long long)v.W * v.H));
+  float in[3] = {0.f, 0.f, 0.f};
+  if (x < d.nx && y < d.ny && z < d.nz) cell_inputs(d, d.at(x + 2, y + 2, z + 2), h1, h2, bdt, nm, in);
+  bf16* dst = in0 + m * 16;
+  dst[0] = __float2bfloat16(in[0]);
+  dst[1] = __float2bfloat16(in[1]);
+  dst[2] = __float2bfloat16(in[2]);
+}
+
+// pc = s1 * out on fluid cells, 0 elsewhere.
+__global__ void k_unpack_domain(Dims d, Vol v, const float* __restrict__ out, const unsigned char* __restrict__ cell,
+                                double s1, double* __restrict__ pc) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)d.n3) return;
+  const int i = (int)(tid % (unsigned)d.NX2);
+  const unsigned t = tid / (unsigned)d.NX2;
+  const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
+  double val = 0.0;
+  if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0)
+    val = s1 * (double)out[((long long)(k - 1) * v.H + (j - 1)) * v.W + (i - 1)];
+  pc[tid] = val;
+}
+
+// One training patch: S^3 cells from origin (i0,j0,k0) (1-based interior cells).
+__global__ void k_capture(Dims d, int S, int i0, int j0, int k0, const double* __restrict__ h1,
+                          const double* __restrict__ h2, const double* __restrict__ bdt,
+                          const double* __restrict__ pc, Norm nm, bf16* __restrict__ din, float* __restrict__ dt) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= (long long)S * S * S) return;
+  const int x = (int)(m % S), y = (int)((m / S) % S), z = (int)(m / ((long long)S * S));
+  const long long o = d.at(i0 + x, j0 + y, k0 + z);
+  float in[3];
+  cell_inputs(d, o, h1, h2, bdt, nm, in);
+  din[m * 4 + 0] = __float2bfloat16(in[0]);
+  din[m * 4 + 1] = __float2bfloat16(in[1]);
+  din[m * 4 + 2] = __float2bfloat16(in[2]);
+  din[m * 4 + 3] = __float2bfloat16(0.f);
+  dt[m] = (float)(pc[o] / nm.s1);
+}
+
+// Gathers a batch of patches into the 16-channel input and the target.
+__global__ void k_gather(long long per, int B, const int* __restrict__ ids, const bf16* __restrict__ ds_in,
+                         const float* __restrict__ ds_t, bf16* __restrict__ in0, float* __restrict__ tgt) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= per * B) return;
+  const int bi = (int)(m / per);
+  const long long v = m % per;
+  const long long src = (long long)ids[bi] * per + v;
+  bf16* dst = in0 + m * 16;
+  for (int c = 0; c < 3; ++c) dst[c] = ds_in[src * 4 + c];
+  tgt[m] = ds_t[src];
+}
+
+// Host-side copy of a batch given as FP32 [B][S^3][3] into the 16-channel input.
+__global__ void k_set_input(long long M, const float* __restrict__ x, bf16* __restrict__ in0) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  for (int c = 0; c < 3; ++c) in0[m * 16 + c] = __float2bfloat16(x[m * 3 + c]);
+}
+
+int norm_for(ib3d_net* n, ib3d_ctx* c, Norm* nm) {
+  NET_CUDA(n, cudaMemsetAsync(n->d_red, 0, 4 * sizeof(double), c->st));
+  const long long ncell = (long long)c->d.nx * c->d.ny * c->d.nz;
+  k_norm_sums<<<(unsigned)((ncell + 255) / 256), 256, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt,
+                                                                   n->d_red);
+  double h[4];
+  NET_CUDA(n, cudaMemcpyAsync(h, n->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  NET_CUDA(n, cudaStreamSynchronize(c->st));
+  if (!(h[3] > 0) || !(h[0] > 0) || !(h[1] > 0) || !(h[2] > 0)) return IB3D_ERR_ARG;
+  nm->s1 = std::sqrt(h[0] / h[3]);
+  nm->s2 = std::sqrt(h[1] / h[3]);
+  nm->s3 = std::sqrt(h[2] / h[3]);
+  return IB3D_OK;
+}
+
+}  // namespace
+
+namespace ib3d {
+// Called by the pressure solve: pc = network prediction (returns nonzero when the
+// history or the normalisation is not available yet; pc is then left unchanged).
+int net_predict_pc(ib3d_ctx* c) {
+  ib3d_net* n = c->net;
+  if (!n || c->hist_valid < 2) return 1;
+  Norm nm;
+  if (norm_for(n, c, &nm) != IB3D_OK) return 1;
+  const Vol v{1, (c->d.nz + 3) / 4 * 4, (c->d.ny + 3) / 4 * 4, (c->d.nx + 3) / 4 * 4};
+  cudaStream_t saved = n->st;
+  n->st = c->st;
+  int rc = ensure_buffers(n, v, false);
+  if (rc) { n->st = saved; return rc; }
+  k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, c->hist[0], c->hist[1], c->bdt, nm,
+                                                                         n->buf.in0);
+  forward(n);
+  k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, n->buf.out, c->cell, nm.s1, c->pc);
+  n->st = saved;
+  c->launches += 18;
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+}  // namespace ib3d
+
+extern "C" {
+
+int ib3d_net_create(ib3d_net** out, uint64_t seed) {
+  if (!out) return IB3D_ERR_ARG;
+  *out = nullptr;
+  ib3d_net* n = new ib3d_net();
+  size_t off = 0;
+  for (int l = 0; l < kL; ++l) {
+    n->L[l] = {kN[l], kK[l], kKreal[l], off, off + (size_t)kN[l] * 27 * kK[l]};
+    off = n->L[l].b + kN[l];
+    off = (off + 7) & ~(size_t)7;    // keep every block 32-byte aligned
+  }
+  n->head = off;
+  n->nparam = off + 17;
+  std::vector<float> hp(n->nparam, 0.0f);
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < kL; ++l) {
+    std::normal_distribution<float> nd(0.0f, std::sqrt(2.0f / (27.0f * kKreal[l])));
+    for (int o = 0; o < kN[l]; ++o)
+      for (int t = 0; t < 27; ++t)
+        for (int k = 0; k < kK[l]; ++k)
+          hp[n->L[l].w + ((size_t)o * 27 + t) * kK[l] + k] = k < kKreal[l] ? nd(rng) : 0.0f;
+  }
+  std::normal_distribution<float> nh(0.0f, 0.01f);
+  for (int q = 0; q < 16; ++q) hp[n->head + q] = nh(rng);
+  bool ok = cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking) == cudaSuccess;
+  float** fb[] = {&n->p, &n->g, &n->m1, &n->m2};
+  for (float** q : fb) ok = ok && cudaMalloc(q, n->nparam * sizeof(float)) == cudaSuccess;
+  ok = ok && cudaMalloc(&n->wf, n->nparam * sizeof(bf16)) == cudaSuccess &&
+       cudaMalloc(&n->wt, n->nparam * sizeof(bf16)) == cudaSuccess &&
+       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, 4 * sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    ib3d_net_destroy(n);
+    return IB3D_ERR_MEMORY;
+  }
+  cudaMemcpy(n->p, hp.data(), n->nparam * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(n->m1, 0, n->nparam * sizeof(float));
+  cudaMemset(n->m2, 0, n->nparam * sizeof(float));
+  cast_weights(n);
+  if (cudaStreamSynchronize(n->st) != cudaSuccess) {
+    ib3d_net_destroy(n);
+    return IB3D_ERR_CUDA;
+  }
+  *out = n;
+  return IB3D_OK;
+}
+
+void ib3d_net_destroy(ib3d_net* n) {
+  if (!n) return;
+  if (n->st) cudaStreamSynchronize(n->st);
+  free_buffers(n->buf);
+  void* ptrs[] = {n->p, n->g, n->m1, n->m2, n->wf, n->wt, n->ds_in, n->ds_t, n->d_loss, n->d_red};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (n->st) cudaStreamDestroy(n->st);
+  delete n;
+}
+
+const char* ib3d_net_last_error(const ib3d_net* n) { return n ? n->err.c_str() : "null network"; }
+
+int64_t ib3d_net_num_params(const ib3d_net* n) { return n ? (int64_t)n->nparam : 0; }
+
+int ib3d_net_get_params(ib3d_net* n, float* out) {
+  if (!n || !out) return IB3D_ERR_ARG;
+  NET_CUDA(n, cudaMemcpy(out, n->p, n->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+  return IB3D_OK;
+}
+
+int ib3d_net_set_params(ib3d_net* n, const float* in) {
+  if (!n || !in) return IB3D_ERR_ARG;
+  NET_CUDA(n, cudaMemcpy(n->p, in, n->nparam * sizeof(float), cudaMemcpyHostToDevice));
+  cast_weights(n);
+  NET_CUDA(n, cudaStreamSynchronize(n->st));
+  return IB3D_OK;
+}
+
+// Loss and parameter gradient of one batch given on the host (x: [B][S^3][3] FP32,
+// target: [B][S^3]); no update. out (may be NULL) receives the network output.
+int ib3d_net_loss_grad(ib3d_net* n, int B, int S, const float* x, const float* target, double* loss, float* grad,
+                       float* out) {
+  if (!n || B < 1 || S < 4 || S % 4 || !x || !target) return IB3D_ERR_ARG;
+  const Vol v{B, S, S, S};
+  int rc = ensure_buffers(n, v, true);
+  if (rc) return rc;
+  const long long M = v.voxels();
+  float* dx = nullptr;
+  NET_CUDA(n, cudaMalloc(&dx, (size_t)M * 3 * sizeof(float)));
+  cudaMemcpyAsync(dx, x, (size_t)M * 3 * sizeof(float), cudaMemcpyHostToDevice, n->st);
+  cudaMemcpyAsync(n->buf.tgt, target, (size_t)M * sizeof(float), cudaMemcpyHostToDevice, n->st);
+  k_set_input<<<(unsigned)((M + 255) / 256), 256, 0, n->st>>>(M, dx, n->buf.in0);
+  cudaMemsetAsync(n->g, 0, n->nparam * sizeof(float), n->st);
+  cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
+  forward(n);
+  mse(n->st, M, n->buf.out, n->buf.tgt, n->buf.gout, n->d_loss);
+  backward(n);
+  if (loss) cudaMemcpyAsync(loss, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
+  if (grad) cudaMemcpyAsync(grad, n->g, n->nparam * sizeof(float), cudaMemcpyDeviceToHost, n->st);
+  if (out) cudaMemcpyAsync(out, n->buf.out, (size_t)M * sizeof(float), cudaMemcpyDeviceToHost, n->st);
+  NET_CUDA(n, cudaStreamSynchronize(n->st));
+  cudaFree(dx);
+  NET_CUDA(n, cudaGetLastError());
+  return IB3D_OK;
+}
+
+// Reserves room for `capacity` training patches of edge S (S a multiple of 4).
+int ib3d_net_dataset_reserve(ib3d_net* n, int S, int64_t capacity) {
+  if (!n || S < 4 || S % 4 || capacity < 1) return IB3D_ERR_ARG;
+  if (n->ds_in) cudaFree(n->ds_in);
+  if (n->ds_t) cudaFree(n->ds_t);
+  n->ds_in = nullptr;
+  n->ds_t = nullptr;
+  const size_t per = (size_t)S * S * S;
+  NET_CUDA(n, cudaMalloc(&n->ds_in, (size_t)capacity * per * 4 * sizeof(bf16)));
+  NET_CUDA(n, cudaMalloc(&n->ds_t, (size_t)capacity * per * sizeof(float)));
+  n->S = S;
+  n->cap = capacity;
+  n->count = 0;
+  return IB3D_OK;
+}
+
+int64_t ib3d_net_dataset_size(const ib3d_net* n) { return n ? n->count : 0; }
+
+// Adds up to npatches random S^3 patches of the context's last step (inputs from
+// the two previous pressures and this step's b/dt, target this step's pc).
+int ib3d_net_capture(ib3d_net* n, ib3d_ctx* c, int npatches, uint64_t seed) {
+  if (!n || !c || npatches < 1 || !n->ds_in) return IB3D_ERR_ARG;
+  if (c->hist_valid < 2) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: fewer than two previous pressures");
+  const int S = n->S;
+  if (S > c->d.nx || S > c->d.ny || S > c->d.nz) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: patch larger than grid");
+  Norm nm;
+  if (norm_for(n, c, &nm) != IB3D_OK) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: zero normalisation");
+  std::mt19937_64 rng(seed);
+  const size_t per = (size_t)S * S * S;
+  for (int q = 0; q < npatches && n->count < n->cap; ++q) {
+    const int i0 = 2 + (int)(rng() % (uint64_t)(c->d.nx - S + 1));
+    const int j0 = 2 + (int)(rng() % (uint64_t)(c->d.ny - S + 1));
+    const int k0 = 2 + (int)(rng() % (uint64_t)(c->d.nz - S + 1));
+    k_capture<<<(unsigned)((per + 255) / 256), 256, 0, c->st>>>(c->d, S, i0, j0, k0, c->hist[0], c->hist[1], c->bdt,
+                                                                c->pc, nm, n->ds_in + n->count * per * 4,
+                                                                n->ds_t + n->count * per);
+    n->count++;
+  }
+  NET_CUDA(n, cudaStreamSynchronize(c->st));
+  NET_CUDA(n, cudaGetLastError());
+  return IB3D_OK;
+}
+
+// `steps` Adam steps (lr, default moments) on random batches of the captured set.
+int ib3d_net_train(ib3d_net* n, int steps, int batch, double lr, uint64_t seed, double* last_loss) {
+  if (!n || steps < 1 || batch < 1 || n->count < 1) return IB3D_ERR_ARG;
+  const int S = n->S;
+  const Vol v{batch, S, S, S};
+  int rc = ensure_buffers(n, v, true);
+  if (rc) return rc;
+  const long long per = (long long)S * S * S, M = v.voxels();
+  int* ids = nullptr;
+  NET_CUDA(n, cudaMalloc(&ids, batch * sizeof(int)));
+  std::mt19937_64 rng(seed);
+  std::vector<int> hid(batch);
+  double loss = 0.0;
+  for (int s = 0; s < steps; ++s) {
+    for (int q = 0; q < batch; ++q) hid[q] = (int)(rng() % (uint64_t)n->count);
+    cudaMemcpyAsync(ids, hid.data(), batch * sizeof(int), cudaMemcpyHostToDevice, n->st);
+    k_gather<<<(unsigned)((M + 255) / 256), 256, 0, n->st>>>(per, batch, ids, n->ds_in, n->ds_t, n->buf.in0,
+                                                            n->buf.tgt);
+    cudaMemsetAsync(n->g, 0, n->nparam * sizeof(float), n->st);
+    cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
+    forward(n);
+    mse(n->st, M, n->buf.out, n->buf.tgt, n->buf.gout, n->d_loss);
+    backward(n);
+    n->step++;
+    adam(n->st, (int)n->nparam, n->p, n->g, n->m1, n->m2, (float)lr, n->step);
+    cast_weights(n);
+    if (s == steps - 1) cudaMemcpyAsync(&loss, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
+    // hid is rewritten next step: wait for the async copy of this step's ids
+    cudaStreamSynchronize(n->st);
+  }
+  cudaFree(ids);
+  NET_CUDA(n, cudaGetLastError());
+  if (last_loss) *last_loss = loss;
+  return IB3D_OK;
+}
+
+// Uses the network as the warm start of ctx's pressure solves (IB3D_WARM_LEARNED).
+int ib3d_attach_net(ib3d_ctx* c, ib3d_net* n) {
+  if (!c) return IB3D_ERR_ARG;
+  c->net = n;
+  return ib3d_enable_history(c);
+}
+
+}  // extern "C"

@@ -52,6 +52,7 @@ extern "C" {
 /* Initial guess of the pressure correction pc at each step. */
 #define IB3D_WARM_ZERO 0     /* pc = 0, as subPcorVcor.f90:19-28 */
 #define IB3D_WARM_PREV 1     /* pc = previous step's pc (linear extrapolation of p) */
+#define IB3D_WARM_LEARNED 2  /* pc = prediction of the attached network (ib3d_attach_net) */
 
 typedef struct ib3d_params {
   double re;            /* Reynolds number (inputdata line 2; rev = 1/re, subReadInput.f90:22) */
@@ -64,7 +65,10 @@ typedef struct ib3d_params {
   int32_t warm_start;   /* IB3D_WARM_* */
   int32_t check_every;  /* sweeps between residual checks (IB3D_CRIT_RESIDUAL); >= 1 */
   int32_t inner_sweeps; /* FP32 sweeps per defect-correction pass (IB3D_PREC_FP32DC) */
-  int32_t sweep_kernel; /* FP32 sweep form: 0 one fused launch per sweep, 1 one launch per colour */
+  int32_t sweep_kernel; /* FP32 sweep layout: 0 colour-packed arrays (even nx), 1 the padded field layout */
+  double omega_inner;   /* relaxation factor of the FP32 inner sweeps (0: use omega). The FP64
+                           defect correction fixes the final accuracy, so the inner solve may use
+                           its own factor. */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
@@ -144,9 +148,10 @@ int ib3d_step(ib3d_ctx* ctx, int first, ib3d_solve_stats* stats, double coef[4])
  * subPcorVcor.f90:33-37, and logs it to iter.dat :60-65). When enabled, every
  * phase records CUDA events on the context's stream; reading synchronizes.
  * ms[]: 0 momentum, 1 boundary conditions, 2 forcing, 3 divergence, 4 FP64 sweeps,
- * 5 FP32 sweeps, 6 residual + accumulation, 7 corrections + copy, 8 drag/lift. */
+ * 5 FP32 sweeps, 6 residual + accumulation, 7 corrections + copy, 8 drag/lift,
+ * 9 network warm start. */
 typedef struct ib3d_timers {
-  double ms[9];
+  double ms[10];
   int64_t sweeps64;   /* FP64 red-black sweeps run */
   int64_t sweeps32;   /* FP32 red-black sweeps run */
   int64_t outer;      /* defect-correction passes */
@@ -165,6 +170,38 @@ void* ib3d_stream(ib3d_ctx* ctx);
 void* ib3d_device_field(ib3d_ctx* ctx, int which);
 /* Blocks until the context's stream is idle. */
 int ib3d_synchronize(ib3d_ctx* ctx);
+
+/* ---- Learned warm start (no counterpart in the reference; configs[3]) --------------
+ * A 3-level 3-D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
+ * activations, FP32 accumulation) predicts each step's pressure correction pc from
+ * the two previous pressures and the step's b/dt; the prediction is the SOR initial
+ * guess and the FP64 stopping test is unchanged. It is trained on the GPU by this
+ * library's own forward, backward and Adam kernels on patches captured from solver
+ * runs. */
+typedef struct ib3d_net ib3d_net;
+int ib3d_net_create(ib3d_net** out, uint64_t seed);   /* He-initialised weights */
+void ib3d_net_destroy(ib3d_net* net);
+const char* ib3d_net_last_error(const ib3d_net* net);
+int64_t ib3d_net_num_params(const ib3d_net* net);
+int ib3d_net_get_params(ib3d_net* net, float* out);
+int ib3d_net_set_params(ib3d_net* net, const float* in);
+/* Loss (mean squared error) and gradient of one batch given on the host: x is
+ * [B][S^3][3] FP32 (x fastest within a patch), target [B][S^3]; S a multiple of 4.
+ * out (may be NULL) receives the prediction. No parameter update. */
+int ib3d_net_loss_grad(ib3d_net* net, int B, int S, const float* x, const float* target, double* loss, float* grad,
+                       float* out);
+/* Training set: room for `capacity` patches of S^3 cells; ib3d_net_capture adds
+ * random patches of a context's last step (after ib3d_step), ib3d_net_train runs
+ * Adam steps on random batches of it. */
+int ib3d_net_dataset_reserve(ib3d_net* net, int S, int64_t capacity);
+int64_t ib3d_net_dataset_size(const ib3d_net* net);
+int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
+int ib3d_net_train(ib3d_net* net, int steps, int batch, double lr, uint64_t seed, double* last_loss);
+/* Keeps the two previous pressures in ctx (needed by capture and by the learned
+ * warm start); ib3d_attach_net calls it. */
+int ib3d_enable_history(ib3d_ctx* ctx);
+/* Network used by IB3D_WARM_LEARNED (NULL detaches). */
+int ib3d_attach_net(ib3d_ctx* ctx, ib3d_net* net);
 
 /* Mixed-precision pressure solve that allocates no memory. No counterpart in the
  * reference: it serves host codes that cannot call cudaMalloc -- a solver whose

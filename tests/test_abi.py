@@ -38,7 +38,7 @@ def test_python_mirror_binds_every_symbol(ib3d, built_lib):
 
 def test_params_struct_layout(ib3d, built_lib):
     p = ib3d.default_params()
-    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6
+    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8
     assert p.omega == 1.99 and p.eps == 1e-5 and p.criterion == ib3d.CRIT_UPDATE
 
 
