@@ -280,6 +280,39 @@ def cpu_sample(pkg, cs, sweeps_per_step: float, threads: int) -> dict:
 
 # ------------------------------------------------------------------ main
 
+def run_poisson(pkg, n: int) -> dict:
+    """Standalone pressure-Poisson solve (tanh-clustered n^3 cube, Neumann on all
+    faces, divergence of a seeded filtered random field, omega 1.85 to a residual of
+    1e-8) in FP64 and in FP32-sweep/FP64-defect-correction form: sweeps/s and the
+    sweep kernels' algorithmic GB/s."""
+    P = pkg.grids.poisson_problem(n, seed=0)
+    out = {"workload": f"standalone Poisson {n}^3, tanh-clustered, all-Neumann, omega 1.85, residual 1e-8",
+           "cells": n ** 3}
+    arms = {"fp64": dict(precision=0, criterion=1, check_every=8),
+            "fp32dc": dict(precision=1, criterion=1, inner_sweeps=256, omega_inner=1.85, sweep_kernel=0)}
+    for name, kw in arms.items():
+        p = pkg.default_params(re=100.0, deltat=1.0, omega=1.85, eps=1e-8, max_sweeps=1_000_000)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        s = pkg.Solver(P["x"], P["y"], P["z"], p)
+        s.set_poisson_coefficients(*P["acoef"])
+        s.set_field("b", P["b"])
+        s.timers_enable(True)
+        st = s.redblack_sor()
+        tm = s.timers_read()
+        sweeps = st["sweeps"]
+        if name == "fp64":
+            t_sweep = tm["sor64_ms"] / max(tm["sweeps64"], 1) * 1e-3
+            gbs = BYTES_SOR64 * n ** 3 / t_sweep / 1e9
+        else:
+            t_sweep = tm["sor32_ms"] / max(tm["sweeps32"], 1) * 1e-3
+            gbs = 2 * BYTES_SOR32_LAUNCH * n ** 3 / t_sweep / 1e9
+        out[name] = {"sweeps": sweeps, "seconds": st["solve_seconds"], "sweeps_per_s": sweeps / st["solve_seconds"],
+                     "final_residual": st["final_err"], "ms_per_sweep": t_sweep * 1e3, "sweep_gbs_algorithmic": gbs}
+        s.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -292,12 +325,25 @@ def main():
     ap.add_argument("--record-sweeps", type=int, default=0,
                     help="write the FP64 sweep counts of the first N steps to oracle/sweeps_<case>.json")
     ap.add_argument("--record-out", default=None, help="output path of --record-sweeps")
+    ap.add_argument("--poisson", type=int, default=0,
+                    help="instead of the step benchmark: the standalone all-Neumann Poisson cube of this edge "
+                         "(omega 1.85, residual 1e-8), FP64 and FP32-sweep forms")
+    ap.add_argument("--set", default="",
+                    help="comma-separated key=value overrides of the FP32-sweep arm's solver parameters")
     ap.add_argument("--arms", default="fast,plain,e2e,cpu",
                     help="comma-separated subset of fast,plain,e2e,cpu (profiling runs use 'fast')")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
     dist = Dist()
     pkg = package()
+    for kv in filter(None, args.set.split(",")):
+        k, v = kv.split("=")
+        FAST[k.strip()] = float(v) if "." in v or "e" in v else int(v)
+    if args.poisson:
+        if dist.rank == 0:
+            print(json.dumps(run_poisson(pkg, args.poisson)), flush=True)
+        dist.close()
+        return
     cs = workload(pkg, args.case)
     threads = os.cpu_count() or 1
 

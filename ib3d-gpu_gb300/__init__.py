@@ -30,6 +30,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMOR
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
 PREC_FP64, PREC_FP32DC = 0, 1
 WARM_ZERO, WARM_PREV, WARM_LEARNED = 0, 1, 2
+INNER_FIXED, INNER_ADAPTIVE = 0, 1
 FIELDS = {"u": 0, "v": 1, "w": 2, "ut": 3, "vt": 4, "wt": 5, "p": 6, "pc": 7, "b": 8}
 _ERRNAMES = {ERR_ARG: "IB3D_ERR_ARG", ERR_CUDA: "IB3D_ERR_CUDA", ERR_MESH: "IB3D_ERR_MESH",
              ERR_PROBE: "IB3D_ERR_PROBE", ERR_NOCONV: "IB3D_ERR_NOCONV", ERR_NONFINITE: "IB3D_ERR_NONFINITE",
@@ -46,12 +47,12 @@ class Params(C.Structure):
     _fields_ = [("re", C.c_double), ("deltat", C.c_double), ("omega", C.c_double), ("eps", C.c_double),
                 ("max_sweeps", C.c_int64), ("criterion", C.c_int32), ("precision", C.c_int32),
                 ("warm_start", C.c_int32), ("check_every", C.c_int32), ("inner_sweeps", C.c_int32),
-                ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double)]
+                ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double), ("inner_schedule", C.c_int32)]
 
 
 class SolveStats(C.Structure):
     _fields_ = [("sweeps", C.c_int64), ("outer", C.c_int64), ("divmax", C.c_double), ("derr_std_st", C.c_double),
-                ("final_err", C.c_double), ("solve_seconds", C.c_double)]
+                ("final_err", C.c_double), ("solve_seconds", C.c_double), ("initial_err", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -79,7 +80,7 @@ _VP = C.c_void_p
 def header_functions() -> list[str]:
     """Names of the functions include/ib3d.h declares."""
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:int|void\*?|char\*?|const char\*)\s*\**\s*(ib3d_\w+)\s*\(",
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:int|int64_t|void\*?|char\*?|const char\*)\s*\**\s*(ib3d_\w+)\s*\(",
                                  text, re.M)))
 
 
@@ -100,6 +101,8 @@ def lib() -> C.CDLL:
         "ib3d_set_mesh": (C.c_int, [_VP, C.c_int64, _D, _D, _D, C.c_int64, _I64, _I64, _I64, C.c_double,
                                     C.c_double, C.c_double, C.c_int64]),
         "ib3d_search": (C.c_int, [_VP, _I64, _I64]),
+        "ib3d_move_body": (C.c_int, [_VP] + [C.c_double] * 6),
+        "ib3d_set_poisson_coefficients": (C.c_int, [_VP, _D, _D, _D]),
         "ib3d_get_search": (C.c_int, [_VP, _I64, _I64, _I64, _D]),
         "ib3d_initial_conditions": (C.c_int, [_VP]),
         "ib3d_upload_fields": (C.c_int, [_VP, _D, _D, _D, _D]),
@@ -112,6 +115,7 @@ def lib() -> C.CDLL:
         "ib3d_velocity_forcing": (C.c_int, [_VP]),
         "ib3d_pressure_forcing": (C.c_int, [_VP]),
         "ib3d_poisson_solver": (C.c_int, [_VP, C.POINTER(SolveStats)]),
+        "ib3d_redblack_sor": (C.c_int, [_VP, C.POINTER(SolveStats)]),
         "ib3d_stress": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_step": (C.c_int, [_VP, C.c_int, C.POINTER(SolveStats), _D]),
         "ib3d_device_field": (_VP, [_VP, C.c_int]),
@@ -227,6 +231,16 @@ class Solver:
         self.counts = dict(zip(("fluid", "solid", "ib", "red", "black"), (int(v) for v in counts)))
         return self.counts
 
+    def set_poisson_coefficients(self, acx, acy, acz):
+        """Replaces Acx/Acy/Acz ((n,3) arrays, the layout coefficientMatrix builds)."""
+        a = [np.asfortranarray(v, dtype=np.float64) for v in (acx, acy, acz)]
+        self._check(self.L.ib3d_set_poisson_coefficients(self._h, *(_dp(v) for v in a)),
+                    "ib3d_set_poisson_coefficients")
+
+    def move_body(self, dx: float, dy: float, dz: float, us: float = 0.0, vs: float = 0.0, ws: float = 0.0):
+        """Prescribed motion: shift the body, set its velocity; search again before stepping."""
+        self._check(self.L.ib3d_move_body(self._h, dx, dy, dz, us, vs, ws), "ib3d_move_body")
+
     def get_search(self) -> dict:
         nib = self.counts["ib"]
         cell = np.zeros(self.shape, dtype=np.int64, order="F")
@@ -311,6 +325,16 @@ class Solver:
         d["rc"] = rc
         return d
 
+    def redblack_sor(self, allow_noconv: bool = False) -> dict:
+        """REDBLACKSOR alone on the b already set (set_field("b", ...))."""
+        st = SolveStats()
+        rc = self.L.ib3d_redblack_sor(self._h, C.byref(st))
+        if not (allow_noconv and rc == ERR_NOCONV):
+            self._check(rc, "ib3d_redblack_sor")
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
     def stress(self, first: bool) -> np.ndarray:
         coef = np.zeros(4, dtype=np.float64)
         self._check(self.L.ib3d_stress(self._h, 1 if first else 0, _dp(coef)), "ib3d_stress")
@@ -365,7 +389,8 @@ class Net:
         self._check(self.L.ib3d_net_set_params(self._h, p.ctypes.data_as(_F)), "ib3d_net_set_params")
 
     def loss_grad(self, x: np.ndarray, target: np.ndarray):
-        """x: [B, S, S, S, 3] (z, y, x, channel), target: [B, S, S, S]."""
+        """x: [B, S, S, S, 4] (z, y, x, channel: previous correction, b/dt, previous
+        pressure, residual of the previous correction), target: [B, S, S, S]."""
         B, S = x.shape[0], x.shape[1]
         x = np.ascontiguousarray(x, dtype=np.float32)
         t = np.ascontiguousarray(target, dtype=np.float32)

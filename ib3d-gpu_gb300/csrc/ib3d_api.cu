@@ -238,7 +238,8 @@ bool valid_params(const ib3d_params* p) {
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
          (p->precision == 0 || p->precision == 1) && (p->warm_start >= 0 && p->warm_start <= 2) &&
          p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
-         (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0));
+         (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
+         (p->inner_schedule == IB3D_INNER_FIXED || p->inner_schedule == IB3D_INNER_ADAPTIVE);
 }
 
 int fail(ib3d_ctx* c, int code, const char* msg) {
@@ -250,6 +251,41 @@ int fail(ib3d_ctx* c, int code, const char* msg) {
 }  // namespace ib3d
 
 using namespace ib3d;
+
+// FP32 copies of the nine Poisson tables (each padded to 8 floats; off32[3*axis+col]
+// is each table's offset) and, for even nx, the x tables regrouped for the
+// colour-packed sweep: hp[((s*3 + col)*nq + g)*4 + e] = Acx(i-1, col) at
+// i = 2 + s + 8g + 2e (0 beyond the row).
+static void poisson32_host(const ib3d_ctx* c, std::vector<float>& h32, std::vector<size_t>& off32,
+                           std::vector<float>& hp) {
+  h32.clear(); off32.clear(); hp.clear();
+  for (int ax = 0; ax < 3; ++ax)
+    for (int q = 0; q < 3; ++q) {
+      off32.push_back(h32.size());
+      for (double x : c->hac[ax][q]) h32.push_back((float)x);
+      while (h32.size() % 8) h32.push_back(0.0f);
+    }
+  const int nx = c->d.nx;
+  if (nx % 2 == 0) {
+    const int nq = ((nx >> 1) + 3) >> 2;
+    hp.assign((size_t)2 * 3 * nq * 4, 0.0f);
+    for (int s = 0; s < 2; ++s)
+      for (int q = 0; q < 3; ++q)
+        for (int g = 0; g < nq; ++g)
+          for (int e = 0; e < 4; ++e) {
+            const long long i = 2 + s + 8ll * g + 2 * e;
+            if (i <= nx + 1) hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = (float)c->hac[0][q][i - 1];
+          }
+  }
+}
+
+static int upload_poisson32(ib3d_ctx* c, const std::vector<float>& h32, const std::vector<float>& hp) {
+  if (cudaMemcpy(c->d_tables32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return IB3D_ERR_CUDA;
+  if (!hp.empty() && cudaMemcpy(c->d_axp, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return IB3D_ERR_CUDA;
+  return IB3D_OK;
+}
 
 extern "C" {
 
@@ -363,40 +399,28 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
     rc = IB3D_ERR_CUDA;
   if (!rc)
     for (auto& f : pk.fix) *f.first = c->d_tables + f.second;
-  // FP32 copies of the Poisson coefficients for the inner solve
+  // FP32 copies of the Poisson coefficients for the inner solve, and the x
+  // coefficients of the colour-packed FP32 sweep grouped by four cells of one colour
   if (!rc) {
-    std::vector<float> h32;
-    std::vector<std::pair<const float**, size_t>> fix32;
-    for (int ax = 0; ax < 3; ++ax)
-      for (int q = 0; q < 3; ++q) {
-        const float** slot = ax == 0 ? &c->g.acx32[q] : ax == 1 ? &c->g.acy32[q] : &c->g.acz32[q];
-        fix32.push_back({slot, h32.size()});
-        for (double x : c->hac[ax][q]) h32.push_back((float)x);
-        while (h32.size() % 8) h32.push_back(0.0f);
-      }
+    std::vector<float> h32, hp;
+    std::vector<size_t> off32;
+    poisson32_host(c, h32, off32, hp);
     if (cudaMalloc(&c->d_tables32, h32.size() * sizeof(float)) != cudaSuccess) rc = IB3D_ERR_MEMORY;
-    if (!rc && cudaMemcpy(c->d_tables32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-      rc = IB3D_ERR_CUDA;
-    if (!rc)
-      for (auto& f : fix32) *f.first = c->d_tables32 + f.second;
-  }
-  // x coefficients of the colour-packed FP32 sweep, grouped by four cells of one colour
-  if (!rc && nx % 2 == 0) {
-    const int nq = (int)(((nx >> 1) + 3) >> 2);
-    std::vector<float> hp((size_t)2 * 3 * nq * 4, 0.0f);
-    for (int s = 0; s < 2; ++s)
-      for (int q = 0; q < 3; ++q)
-        for (int g = 0; g < nq; ++g)
-          for (int e = 0; e < 4; ++e) {
-            const long long i = 2 + s + 8ll * g + 2 * e;
-            if (i <= nx + 1) hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = (float)c->hac[0][q][i - 1];
-          }
-    if (cudaMalloc(&c->d_axp, hp.size() * sizeof(float)) != cudaSuccess) rc = IB3D_ERR_MEMORY;
-    if (!rc && cudaMemcpy(c->d_axp, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-      rc = IB3D_ERR_CUDA;
-    if (!rc)
-      for (int s = 0; s < 2; ++s)
-        for (int q = 0; q < 3; ++q) c->g.axp[s][q] = reinterpret_cast<const float4*>(c->d_axp) + ((size_t)s * 3 + q) * nq;
+    if (!rc && !hp.empty() && cudaMalloc(&c->d_axp, hp.size() * sizeof(float)) != cudaSuccess) rc = IB3D_ERR_MEMORY;
+    if (!rc) {
+      for (int ax = 0; ax < 3; ++ax)
+        for (int q = 0; q < 3; ++q) {
+          const float** slot = ax == 0 ? &c->g.acx32[q] : ax == 1 ? &c->g.acy32[q] : &c->g.acz32[q];
+          *slot = c->d_tables32 + off32[3 * ax + q];
+        }
+      if (!hp.empty()) {
+        const int nq = (int)(((nx >> 1) + 3) >> 2);
+        for (int s = 0; s < 2; ++s)
+          for (int q = 0; q < 3; ++q)
+            c->g.axp[s][q] = reinterpret_cast<const float4*>(c->d_axp) + ((size_t)s * 3 + q) * nq;
+      }
+      rc = upload_poisson32(c, h32, hp);
+    }
   }
   if (!rc) {
     const int S = (int)std::max(nx, std::max(ny, nz)) + 3;
@@ -429,12 +453,35 @@ void ib3d_destroy(ib3d_ctx* c) {
   void* ptrs[] = {c->d_tables, c->d_tables32, c->d_fast, c->d_axp, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
-                  c->hist[0], c->hist[1]};
+                  c->hist[0], c->hist[1], c->r_hist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
+}
+
+int ib3d_set_poisson_coefficients(ib3d_ctx* c, const double* acx, const double* acy, const double* acz) {
+  if (!c || !acx || !acy || !acz) return IB3D_ERR_ARG;
+  const int n[3] = {c->d.nx, c->d.ny, c->d.nz};
+  const double* src[3] = {acx, acy, acz};
+  for (int ax = 0; ax < 3; ++ax)
+    for (int q = 0; q < 3; ++q)
+      for (int i = 1; i <= n[ax]; ++i)
+        if (!std::isfinite(src[ax][(size_t)q * n[ax] + (i - 1)]))
+          return fail(c, IB3D_ERR_ARG, "ib3d_set_poisson_coefficients: non-finite coefficient");
+  IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  for (int ax = 0; ax < 3; ++ax)
+    for (int q = 0; q < 3; ++q) {
+      std::vector<double>& h = c->hac[ax][q];
+      for (int i = 1; i <= n[ax]; ++i) h[i] = src[ax][(size_t)q * n[ax] + (i - 1)];   // (n,3) column-major
+      const double* dev = ax == 0 ? c->g.acx[q] : ax == 1 ? c->g.acy[q] : c->g.acz[q];
+      IB3D_CUDA(c, cudaMemcpy(const_cast<double*>(dev), h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  std::vector<float> h32, hp;
+  std::vector<size_t> off32;
+  poisson32_host(c, h32, off32, hp);
+  return upload_poisson32(c, h32, hp);
 }
 
 int ib3d_set_mesh(ib3d_ctx* c, int64_t nnodes, const double* xn, const double* yn, const double* zn, int64_t nelems,
@@ -478,6 +525,26 @@ int ib3d_set_mesh(ib3d_ctx* c, int64_t nnodes, const double* xn, const double* y
     if (!std::isfinite(x)) return fail(c, IB3D_ERR_MESH, "ib3d_set_mesh: degenerate triangle (zero area)");
   c->searched = false;
   c->have_scache = false;
+  return IB3D_OK;
+}
+
+int ib3d_move_body(ib3d_ctx* c, double dx, double dy, double dz, double us, double vs, double ws) {
+  if (!c) return IB3D_ERR_ARG;
+  if (!c->d_surf) return fail(c, IB3D_ERR_ARG, "ib3d_move_body: call ib3d_set_mesh first");
+  const double v[6] = {dx, dy, dz, us, vs, ws};
+  for (double x : v)
+    if (!std::isfinite(x)) return fail(c, IB3D_ERR_ARG, "ib3d_move_body: non-finite shift or velocity");
+  int rc = run_move_body(c, dx, dy, dz);
+  if (rc) return rc;
+  const double now[3] = {us, vs, ws};
+  for (int q = 0; q < 3; ++q) {
+    // the first move has no previous velocity: no acceleration term
+    c->bprev[q] = c->motion.moving ? c->motion.vel[q] : now[q];
+    c->motion.vel[q] = now[q];
+  }
+  c->motion.moving = 1;
+  c->searched = false;     // the flags and ghost points belong to the old position
+  c->have_scache = false;  // and so do the drag probes
   return IB3D_OK;
 }
 
@@ -658,6 +725,10 @@ int ib3d_enable_history(ib3d_ctx* c) {
       IB3D_CUDA(c, cudaMalloc(&c->hist[q], (size_t)c->d.n3 * sizeof(double)));
       IB3D_CUDA(c, cudaMemsetAsync(c->hist[q], 0, (size_t)c->d.n3 * sizeof(double), c->st));
     }
+  if (!c->r_hist) {
+    IB3D_CUDA(c, cudaMalloc(&c->r_hist, (size_t)c->d.n3 * sizeof(float)));
+    IB3D_CUDA(c, cudaMemsetAsync(c->r_hist, 0, (size_t)c->d.n3 * sizeof(float), c->st));
+  }
   c->hist_valid = 0;
   return IB3D_OK;
 }
@@ -677,6 +748,10 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
   // divergence writes its max into ctl->aux; copy it aside before the SOR resets ctl
   IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
   launch_divergence(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  if (c->r_hist) {
+    PhaseScope ps(c, PH_NET);
+    net_hist_residual(c);   // the current guess's residual: a network input and a capture input
+  }
   if (c->prm.warm_start == IB3D_WARM_LEARNED) {
     PhaseScope ps(c, PH_NET);
     net_predict_pc(c);   // until two previous pressures exist, pc keeps the previous step's value
@@ -712,6 +787,30 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
     c->err = "ib3d_poisson_solver: non-finite divergence or steady-state indicator";
     return IB3D_ERR_NONFINITE;
   }
+  return rc;
+}
+
+int ib3d_redblack_sor(ib3d_ctx* c, ib3d_solve_stats* stats) {
+  if (!c) return IB3D_ERR_ARG;
+  ib3d_solve_stats st{};
+  IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
+  launch_bdt(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->st);
+  const int rc = c->prm.precision == IB3D_PREC_FP32DC ? run_sor_fp32dc(c, &st) : run_sor_fp64(c, &st);
+  cudaEventRecord(e1, c->st);
+  const cudaError_t ce = cudaStreamSynchronize(c->st);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ce != cudaSuccess) return fail(c, IB3D_ERR_CUDA, cudaGetErrorString(ce));
+  st.solve_seconds = ms * 1e-3;
+  if (stats) *stats = st;
+  if (rc == IB3D_ERR_NOCONV) c->err = "ib3d_redblack_sor: SOR reached max_sweeps";
+  if (rc == IB3D_ERR_NONFINITE) c->err = "ib3d_redblack_sor: non-finite SOR error measure";
   return rc;
 }
 

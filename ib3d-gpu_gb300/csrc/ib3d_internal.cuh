@@ -64,6 +64,16 @@ struct SolveCtl {
   double last_res;            // last residual measured
 };
 
+// Body motion seen by the forcing: the surface velocity (usurf, vsurf, wsurf of
+// subForcing.f90:144-145, 228-229, 312-313, 397-398, 482-483, 566-567, set to the
+// body velocity instead of 0) and the acceleration term of dpdn (:20), per axis
+// acc[q] = -(v_curr - v_prev)/deltat. moving = 0 keeps the reference's fixed body.
+struct Motion {
+  int moving;
+  double vel[3];
+  double acc[3];
+};
+
 // Per-op data of the ghost-point schedule. An op is one ghost value: six per
 // immersed-boundary cell for the velocity (blocks U2,U1,V2,V1,W2,W1 in
 // subForcing.f90's order) and one for the pressure.
@@ -123,6 +133,8 @@ struct ib3d_ctx {
   double* d_nodes = nullptr;  // 3*nnodes shifted node coordinates (x block, y block, z block)
   int* d_tri = nullptr;       // 3*nelems 1-based node ids
   double* d_surf = nullptr;   // 9*nelems: xc,yc,zc,cosA,cosB,cosG,alpha3,beta3,gamma3
+  ib3d::Motion motion{};      // prescribed body motion (ib3d_move_body)
+  double bprev[3] = {0, 0, 0};
 
   // search results
   bool searched = false;
@@ -151,6 +163,10 @@ struct ib3d_ctx {
   // previous pressures for the learned warm start: hist[0] = p^{n-1}, hist[1] = p^{n-2}
   double* hist[2] = {nullptr, nullptr};
   int hist_valid = 0;
+  // residual of the previous correction against this step's right-hand side divided
+  // by the diagonal (FP32, padded layout, 0 off the fluid cells), kept for the
+  // network and for capture
+  float* r_hist = nullptr;
   ib3d_net* net = nullptr;
 
   // phase timers (ib3d_timers_*) and the launch counter
@@ -170,6 +186,7 @@ struct ib3d_ctx {
 namespace ib3d {
 // k_pressure.cu
 void launch_divergence(ib3d_ctx* c, bool zero_pc);
+void launch_bdt(ib3d_ctx* c, bool zero_pc);
 int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st);
 int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st);
 void launch_correct(ib3d_ctx* c);
@@ -192,7 +209,10 @@ int run_pressure_forcing(ib3d_ctx* c);
 int run_stress(ib3d_ctx* c, int first, double coef[4]);
 
 // unet.cu: pc = the attached network's prediction; nonzero when not available yet
+int run_move_body(ib3d_ctx* c, double dx, double dy, double dz);
 int net_predict_pc(ib3d_ctx* c);
+// unet.cu: r_hist = ((b/dt) - A pc) / diag(A) for the current pc
+void net_hist_residual(ib3d_ctx* c);
 
 // error helper: records the message and returns IB3D_ERR_CUDA
 int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where);

@@ -447,7 +447,8 @@ __global__ void k_force_vel(Grid1D g, const int* __restrict__ order, int off, in
                             const double* __restrict__ nd, const double* __restrict__ surf, int nib, int ne,
                             const int* __restrict__ brk, const int* __restrict__ rd_idx,
                             const int* __restrict__ rd_src, const double* __restrict__ ut,
-                            const double* __restrict__ vt, const double* __restrict__ wt, double* out) {
+                            const double* __restrict__ vt, const double* __restrict__ wt, Motion mo,
+                            double* out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
   const int q = order[off + t];
@@ -467,19 +468,20 @@ __global__ void k_force_vel(Grid1D g, const int* __restrict__ order, int off, in
   const int e = o.nel - 1;
   const double dndn = pe[1] * surf[3 * ne + e] + pe[2] * surf[4 * ne + e] + pe[3] * surf[5 * ne + e];
   const double n1 = o.pt1 + o.sd;
-  const double surfv = 0.0;                                           // usurf = 0, :145
+  const double surfv = mo.moving ? mo.vel[gb.field] : 0.0;           // usurf = u_curr (:144) or 0 (:145)
   const double cval = surfv;
   const double bval = 2.0 / n1 * (pe[0] - surfv) - dndn;              // :222
   const double aval = dndn / n1 - (pe[0] - surfv) / (n1 * n1);        // :223
   out[q] = aval * (o.sd * o.sd) + bval * o.sd + cval;                 // :224
 }
 
-// One dependency level of pressureForcing1 (subForcing.f90:18-98), dpdn = 0.
+// One dependency level of pressureForcing1 (subForcing.f90:18-98); dpdn = 0 for a
+// fixed body (:11), the body acceleration along the normal for a moving one (:20).
 __global__ void k_force_p(Grid1D g, const int* __restrict__ order, int off, int cnt, const int* __restrict__ iblist,
                           const int* __restrict__ nelp, const double* __restrict__ nd,
                           const double* __restrict__ surf, int nib, int ne, const int* __restrict__ brk,
                           const int* __restrict__ rd_idx, const int* __restrict__ rd_src,
-                          const double* __restrict__ p, double* out) {
+                          const double* __restrict__ p, Motion mo, double* out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
   const int n = order[off + t];
@@ -498,7 +500,9 @@ __global__ void k_force_p(Grid1D g, const int* __restrict__ order, int off, int 
   }
   double pe[4];
   probe_eval(f, g.xp, g.yp, g.zp, brk[3 * n], brk[3 * n + 1], brk[3 * n + 2], px, py, pz, pe);
-  const double dpdn = 0.0;
+  const double dpdn = mo.moving ? (mo.acc[0] * surf[3 * ne + e] + mo.acc[1] * surf[4 * ne + e]) +
+                                      mo.acc[2] * surf[5 * ne + e]
+                                : 0.0;
   const double dpdn_e = pe[1] * surf[3 * ne + e] + pe[2] * surf[4 * ne + e] + pe[3] * surf[5 * ne + e];
   const double n1 = pt1 + sd;
   const double bval = dpdn;
@@ -613,6 +617,23 @@ __global__ void k_stress_sum(const double* __restrict__ contrib, int ne, double*
 }
 
 // ------------------------------------------------------------------- host side
+
+// shiftSurfaceNodesMovingbody's node loop (subSearch.f90:64-73): x = xr + xmove.
+__global__ void k_shift_nodes(double* __restrict__ nodes, int nn, double dx, double dy, double dz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const double xr = nodes[i], yr = nodes[nn + i], zr = nodes[2 * nn + i];
+  nodes[i] = xr + dx;
+  nodes[nn + i] = yr + dy;
+  nodes[2 * nn + i] = zr + dz;
+}
+
+int run_move_body(ib3d_ctx* c, double dx, double dy, double dz) {
+  k_shift_nodes<<<nblk(c->nnodes), kBlock, 0, c->st>>>(c->d_nodes, (int)c->nnodes, dx, dy, dz);
+  IB3D_CUDA(c, cudaGetLastError());
+  c->launches += 2;
+  return run_surface_norm(c);
+}
 
 int run_surface_norm(ib3d_ctx* c) {
   k_surface_norm<<<nblk(c->nelems), kBlock, 0, c->st>>>(c->d_nodes, c->d_tri, (int)c->nnodes, (int)c->nelems,
@@ -773,7 +794,7 @@ int run_velocity_forcing(ib3d_ctx* c) {
     if (cnt <= 0) continue;
     k_force_vel<<<nblk(cnt), kBlock, 0, c->st>>>(c->g, s.order, off, cnt, c->d_iblist, c->d_nelp, c->d_nd, c->d_surf,
                                                  c->nib, (int)c->nelems, s.brk, s.rd_idx, s.rd_src, c->ut, c->vt,
-                                                 c->wt, s.out);
+                                                 c->wt, c->motion, s.out);
   }
   if (s.nfinal > 0)
     k_force_scatter<<<nblk(s.nfinal), kBlock, 0, c->st>>>(s.final_ops, s.nfinal, s.tgt, s.out, 1, c->ut, c->vt,
@@ -785,12 +806,14 @@ int run_velocity_forcing(ib3d_ctx* c) {
 int run_pressure_forcing(ib3d_ctx* c) {
   PhaseScope ps(c, PH_FORCING);
   ForceSched& s = c->fp;
+  for (int q = 0; q < 3; ++q) c->motion.acc[q] = -(c->motion.vel[q] - c->bprev[q]) / c->prm.deltat;   // :20
   c->launches += s.nlevels + (s.nfinal > 0 ? 1 : 0);
   for (int l = 0; l < s.nlevels; ++l) {
     const int off = s.level_off[l], cnt = s.level_off[l + 1] - off;
     if (cnt <= 0) continue;
     k_force_p<<<nblk(cnt), kBlock, 0, c->st>>>(c->g, s.order, off, cnt, c->d_iblist, c->d_nelp, c->d_nd, c->d_surf,
-                                               c->nib, (int)c->nelems, s.brk, s.rd_idx, s.rd_src, c->p, s.out);
+                                               c->nib, (int)c->nelems, s.brk, s.rd_idx, s.rd_src, c->p, c->motion,
+                                               s.out);
   }
   if (s.nfinal > 0)
     k_force_scatter<<<nblk(s.nfinal), kBlock, 0, c->st>>>(s.final_ops, s.nfinal, s.tgt, s.out, 0, c->p, nullptr,

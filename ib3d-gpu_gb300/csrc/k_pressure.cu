@@ -11,6 +11,8 @@
 // bit-identical to the serial oracle. Kernels address the reference's padded
 // Fortran layout directly and mask by the uint8 cell flags instead of gathering
 // through int64 index lists.
+#include <cmath>
+
 #include "ib3d_internal.cuh"
 
 namespace ib3d {
@@ -327,6 +329,22 @@ void launch_divergence(ib3d_ctx* c, bool zero_pc) {
                                                         c->pc, c->prm.deltat, zero_pc ? 1 : 0, &c->ctl->aux);
 }
 
+// b/dt from a b set by the caller (the quotient the sweeps use), and pc = 0 for a
+// zero initial guess.
+__global__ void k_bdt(long long n3, const double* __restrict__ b, double* __restrict__ bdt,
+                      double* __restrict__ pc, double deltat, int zero_pc) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n3) return;
+  bdt[idx] = b[idx] / deltat;
+  if (zero_pc) pc[idx] = 0.0;
+}
+
+void launch_bdt(ib3d_ctx* c, bool zero_pc) {
+  PhaseScope ps(c, PH_DIVERGENCE);
+  c->launches += 1;
+  k_bdt<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d.n3, c->b, c->bdt, c->pc, c->prm.deltat, zero_pc ? 1 : 0);
+}
+
 void launch_correct(ib3d_ctx* c) {
   PhaseScope ps(c, PH_CORRECT);
   c->launches += 1;
@@ -442,6 +460,8 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   if (rc) return rc;
   if (!packed) IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
   long long sweeps = 0, outer = 0;
+  int batch = inner;
+  double prev_res = 0.0;
   for (;;) {
     {
       PhaseScope ps(c, PH_RESIDUAL);
@@ -453,11 +473,23 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);
     if (rc) return rc;
+    const double res = c->h_ctl->last_res;
+    if (outer == 0) st->initial_err = res;
     if (c->h_ctl->done) break;
+    if (P.inner_schedule == IB3D_INNER_ADAPTIVE && outer > 0 && res > 0.0 && res < prev_res) {
+      // log residual reduction per sweep over the last pass, and the sweeps that
+      // rate needs to reach eps (with a margin), at most four decades per pass
+      const double rate = std::log(res / prev_res) / batch;
+      const double need = std::log(P.eps / res) / rate;
+      const double cap = std::log(1e-4) / rate;
+      batch = (int)std::min(std::max(std::min(1.08 * need + 8.0, cap), 16.0), 65536.0);
+    }
+    if (sweeps + batch > P.max_sweeps) batch = (int)std::max(1ll, P.max_sweeps - sweeps);
+    prev_res = res;
     {
       PhaseScope ps(c, PH_SOR32);
-      c->launches += 2 * inner;
-      for (int q = 0; q < inner; ++q) {
+      c->launches += 2 * batch;
+      for (int q = 0; q < batch; ++q) {
         if (packed) {
           launch_sor32_packed(c, 0, om, om1);
           launch_sor32_packed(c, 1, om, om1);
@@ -473,7 +505,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       if (packed) launch_accumulate_packed(c);
       else k_accumulate<<<nblocks(d.n3), kBlock, 0, c->st>>>(d.n3, c->pc, c->e32);
     }
-    sweeps += inner;
+    sweeps += batch;
     ++outer;
   }
   st->sweeps = c->h_ctl->nsweeps;

@@ -3,11 +3,16 @@
 // concatenations, 1x1 head; 0.36 M parameters) in BF16 with FP32 accumulation,
 // trained with Adam on snapshots the solver generates.
 //
-// Inputs per cell: (p^{n-1} - p^{n-2})/s1, (b/dt)^n/s2, p^{n-1}/s3 with s1, s2, s3
-// the RMS of each over the fluid cells (the difference is taken in FP64 before the
-// cast to BF16, which would otherwise erase it). Output: the pressure correction
-// pc^n/s1, used as the SOR initial guess; the FP64 defect-correction loop still
-// stops at the same FP64 residual, so a poor guess only costs sweeps.
+// Inputs per cell: (p^{n-1} - p^{n-2})/s1 (the previous correction pc^{n-1}),
+// (b/dt)^n/s2, p^{n-1}/s3, and r/s4 with r = ((b/dt)^n - A pc^{n-1})/diag(A) the FP64
+// residual of the previous correction against this step's right-hand side;
+// s1..s4 are the RMS of each over the fluid cells. Differences are taken in FP64
+// before the cast to BF16, which would otherwise erase them (b/dt and A pc^{n-1}
+// agree to several digits). Output: the change of the correction,
+// (pc^n - pc^{n-1})/s1, so that the guess is pc^{n-1} + s1 * output: a network
+// with a zero head reproduces the previous-correction warm start exactly, and the
+// FP64 defect-correction loop still stops at the same FP64 residual, so a poor
+// guess only costs sweeps.
 #include <algorithm>
 #include <cmath>
 #include <random>
@@ -25,11 +30,12 @@ struct Layer {
   int N, K, Kreal;
   size_t w, b;   // offsets of the FP32 weights [N][27][K] and biases [N] in the parameter vector
 };
+constexpr int kInputs = 4;   // input channels per cell (see the file header)
 // conv1a conv1b | conv2a conv2b | conv3a conv3b | conv4a conv4b | conv5a conv5b
 constexpr int kL = 10;
 const int kN[kL] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16};
 const int kK[kL] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16};
-const int kKreal[kL] = {3, 16, 16, 32, 32, 64, 96, 32, 48, 16};
+const int kKreal[kL] = {kInputs, 16, 16, 32, 32, 64, 96, 32, 48, 16};
 
 struct Buffers {
   Vol v1{}, v2{}, v3{};
@@ -187,11 +193,13 @@ void cast_weights(ib3d_net* n) {
 
 // ------------------------------------------------------------- data kernels
 
-// RMS inputs over fluid cells: sums of (h1-h2)^2, (b/dt)^2, h1^2 and the fluid count.
+// RMS inputs over fluid cells: sums of (h1-h2)^2, (b/dt)^2, h1^2, r^2 and the
+// fluid count.
 __global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, const double* __restrict__ h1,
-                            const double* __restrict__ h2, const double* __restrict__ bdt, double* sums) {
+                            const double* __restrict__ h2, const double* __restrict__ bdt,
+                            const float* __restrict__ r, double* sums) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
-  double s[4] = {0, 0, 0, 0};
+  double s[5] = {0, 0, 0, 0, 0};
   if (tid < (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) {
     const int i = (int)(tid % (unsigned)d.nx) + 2;
     const unsigned t = tid / (unsigned)d.nx;
@@ -199,10 +207,11 @@ __global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, cons
     const long long o = d.at(i, j, k);
     if (cell[o] == 0) {
       const double dp = h1[o] - h2[o];
-      s[0] = dp * dp; s[1] = bdt[o] * bdt[o]; s[2] = h1[o] * h1[o]; s[3] = 1.0;
+      const double rr = (double)r[o];
+      s[0] = dp * dp; s[1] = bdt[o] * bdt[o]; s[2] = h1[o] * h1[o]; s[3] = rr * rr; s[4] = 1.0;
     }
   }
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 5; ++q) {
     double x = s[q];
     for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
     if ((threadIdx.x & 31) == 0 && x != 0.0) atomicAdd(&sums[q], x);
@@ -210,35 +219,64 @@ __global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, cons
 }
 
 struct Norm {
-  double s1, s2, s3;
+  double s1, s2, s3, s4;
 };
 
-// Input channels of one cell (see the file header); channels 3..15 are zero.
-__device__ __forceinline__ void cell_inputs(const Dims& d, long long o, const double* h1, const double* h2,
-                                            const double* bdt, Norm nm, float in[3]) {
+// Input channels of one cell (see the file header); channels kInputs..15 are zero.
+__device__ __forceinline__ void cell_inputs(long long o, const double* h1, const double* h2, const double* bdt,
+                                            const float* r, Norm nm, float in[kInputs]) {
   in[0] = (float)((h1[o] - h2[o]) / nm.s1);
   in[1] = (float)(bdt[o] / nm.s2);
   in[2] = (float)(h1[o] / nm.s3);
+  in[3] = (float)((double)r[o] / nm.s4);
+}
+
+// r = ((b/dt) - A pc) / diag(A) at the fluid cells (the FP64 residual of the defect
+// correction, scaled as one Jacobi update), 0 elsewhere: the previous correction's
+// residual against this step's right-hand side, taken before the guess is replaced.
+// Dividing by the diagonal takes out the local grid spacing (A ~ 1/h^2), so the
+// input means the same on the fine core and the stretched far field.
+__global__ void __launch_bounds__(kBlock) k_hist_residual(Dims d, Grid1D g, const double* __restrict__ bdt,
+                                                          const double* __restrict__ pc,
+                                                          const unsigned char* __restrict__ cell,
+                                                          float* __restrict__ r) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)d.n3) return;
+  const int i = (int)(tid % (unsigned)d.NX2);
+  const unsigned t = tid / (unsigned)d.NX2;
+  const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
+  float out = 0.f;
+  if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0) {
+    // padded index (i, j, k) 0-based is the 1-based cell (i+1, j+1, k+1)
+    const long long idx = tid, sy = d.NX2, sz = (long long)d.NX2 * d.NY2;
+    const double num = bdt[idx] - g.acx[0][i] * pc[idx - 1] - g.acx[2][i] * pc[idx + 1] -
+                       g.acy[0][j] * pc[idx - sy] - g.acy[2][j] * pc[idx + sy] - g.acz[0][k] * pc[idx - sz] -
+                       g.acz[2][k] * pc[idx + sz];
+    const double diag = g.acx[1][i] + g.acy[1][j] + g.acz[1][k];
+    out = (float)((num - diag * pc[idx]) / diag);
+  }
+  r[tid] = out;
 }
 
 // Full-domain input volume (1 x D x H x W with the interior at the origin, padded
 // with zeros to multiples of 4).
 __global__ void k_pack_domain(Dims d, Vol v, const double* __restrict__ h1, const double* __restrict__ h2,
-                              const double* __restrict__ bdt, Norm nm, bf16* __restrict__ in0) {
+                              const double* __restrict__ bdt, const float* __restrict__ r, Norm nm,
+                              bf16* __restrict__ in0) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= v.voxels()) return;
   const int x = (int)(m % v.W), y = (int)((m / v.W) % v.H), z = (int)(m / ((long long)v.W * v.H));
-  float in[3] = {0.f, 0.f, 0.f};
-  if (x < d.nx && y < d.ny && z < d.nz) cell_inputs(d, d.at(x + 2, y + 2, z + 2), h1, h2, bdt, nm, in);
+  float in[kInputs] = {};
+  if (x < d.nx && y < d.ny && z < d.nz) cell_inputs(d.at(x + 2, y + 2, z + 2), h1, h2, bdt, r, nm, in);
   bf16* dst = in0 + m * 16;
-  dst[0] = __float2bfloat16(in[0]);
-  dst[1] = __float2bfloat16(in[1]);
-  dst[2] = __float2bfloat16(in[2]);
+#pragma unroll
+  for (int c = 0; c < kInputs; ++c) dst[c] = __float2bfloat16(in[c]);
 }
 
-// pc = s1 * out on fluid cells, 0 elsewhere.
+// pc = (p^{n-1} - p^{n-2}) + s1 * out on fluid cells, 0 elsewhere.
 __global__ void k_unpack_domain(Dims d, Vol v, const float* __restrict__ out, const unsigned char* __restrict__ cell,
-                                double s1, double* __restrict__ pc) {
+                                const double* __restrict__ h1, const double* __restrict__ h2, double s1,
+                                double* __restrict__ pc) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (unsigned)d.n3) return;
   const int i = (int)(tid % (unsigned)d.NX2);
@@ -246,25 +284,26 @@ __global__ void k_unpack_domain(Dims d, Vol v, const float* __restrict__ out, co
   const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
   double val = 0.0;
   if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0)
-    val = s1 * (double)out[((long long)(k - 1) * v.H + (j - 1)) * v.W + (i - 1)];
+    val = (h1[tid] - h2[tid]) + s1 * (double)out[((long long)(k - 1) * v.H + (j - 1)) * v.W + (i - 1)];
   pc[tid] = val;
 }
 
 // One training patch: S^3 cells from origin (i0,j0,k0) (1-based interior cells).
 __global__ void k_capture(Dims d, int S, int i0, int j0, int k0, const double* __restrict__ h1,
                           const double* __restrict__ h2, const double* __restrict__ bdt,
-                          const double* __restrict__ pc, Norm nm, bf16* __restrict__ din, float* __restrict__ dt) {
+                          const float* __restrict__ r, const double* __restrict__ pc,
+                          const unsigned char* __restrict__ cell, Norm nm, bf16* __restrict__ din,
+                          float* __restrict__ dt) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= (long long)S * S * S) return;
   const int x = (int)(m % S), y = (int)((m / S) % S), z = (int)(m / ((long long)S * S));
   const long long o = d.at(i0 + x, j0 + y, k0 + z);
-  float in[3];
-  cell_inputs(d, o, h1, h2, bdt, nm, in);
-  din[m * 4 + 0] = __float2bfloat16(in[0]);
-  din[m * 4 + 1] = __float2bfloat16(in[1]);
-  din[m * 4 + 2] = __float2bfloat16(in[2]);
-  din[m * 4 + 3] = __float2bfloat16(0.f);
-  dt[m] = (float)(pc[o] / nm.s1);
+  float in[kInputs];
+  cell_inputs(o, h1, h2, bdt, r, nm, in);
+#pragma unroll
+  for (int c = 0; c < kInputs; ++c) din[m * kInputs + c] = __float2bfloat16(in[c]);
+  // target: the change of the correction (0 where the solve holds pc at 0)
+  dt[m] = cell[o] == 0 ? (float)((pc[o] - (h1[o] - h2[o])) / nm.s1) : 0.f;
 }
 
 // Gathers a batch of patches into the 16-channel input and the target.
@@ -276,35 +315,43 @@ __global__ void k_gather(long long per, int B, const int* __restrict__ ids, cons
   const long long v = m % per;
   const long long src = (long long)ids[bi] * per + v;
   bf16* dst = in0 + m * 16;
-  for (int c = 0; c < 3; ++c) dst[c] = ds_in[src * 4 + c];
+  for (int c = 0; c < kInputs; ++c) dst[c] = ds_in[src * kInputs + c];
   tgt[m] = ds_t[src];
 }
 
-// Host-side copy of a batch given as FP32 [B][S^3][3] into the 16-channel input.
+// Host-side copy of a batch given as FP32 [B][S^3][kInputs] into the 16-channel input.
 __global__ void k_set_input(long long M, const float* __restrict__ x, bf16* __restrict__ in0) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= M) return;
-  for (int c = 0; c < 3; ++c) in0[m * 16 + c] = __float2bfloat16(x[m * 3 + c]);
+  for (int c = 0; c < kInputs; ++c) in0[m * 16 + c] = __float2bfloat16(x[m * kInputs + c]);
 }
 
 int norm_for(ib3d_net* n, ib3d_ctx* c, Norm* nm) {
-  NET_CUDA(n, cudaMemsetAsync(n->d_red, 0, 4 * sizeof(double), c->st));
+  NET_CUDA(n, cudaMemsetAsync(n->d_red, 0, 5 * sizeof(double), c->st));
   const long long ncell = (long long)c->d.nx * c->d.ny * c->d.nz;
   k_norm_sums<<<(unsigned)((ncell + 255) / 256), 256, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt,
-                                                                   n->d_red);
-  double h[4];
+                                                                   c->r_hist, n->d_red);
+  double h[5];
   NET_CUDA(n, cudaMemcpyAsync(h, n->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
   NET_CUDA(n, cudaStreamSynchronize(c->st));
-  if (!(h[3] > 0) || !(h[0] > 0) || !(h[1] > 0) || !(h[2] > 0)) return IB3D_ERR_ARG;
-  nm->s1 = std::sqrt(h[0] / h[3]);
-  nm->s2 = std::sqrt(h[1] / h[3]);
-  nm->s3 = std::sqrt(h[2] / h[3]);
+  for (int q = 0; q < 5; ++q)
+    if (!(h[q] > 0)) return IB3D_ERR_ARG;
+  nm->s1 = std::sqrt(h[0] / h[4]);
+  nm->s2 = std::sqrt(h[1] / h[4]);
+  nm->s3 = std::sqrt(h[2] / h[4]);
+  nm->s4 = std::sqrt(h[3] / h[4]);
   return IB3D_OK;
 }
 
 }  // namespace
 
 namespace ib3d {
+void net_hist_residual(ib3d_ctx* c) {
+  k_hist_residual<<<(unsigned)((c->d.n3 + kBlock - 1) / kBlock), kBlock, 0, c->st>>>(c->d, c->g, c->bdt, c->pc, c->cell,
+                                                                                    c->r_hist);
+  c->launches += 1;
+}
+
 // Called by the pressure solve: pc = network prediction (returns nonzero when the
 // history or the normalisation is not available yet; pc is then left unchanged).
 int net_predict_pc(ib3d_ctx* c) {
@@ -317,10 +364,11 @@ int net_predict_pc(ib3d_ctx* c) {
   n->st = c->st;
   int rc = ensure_buffers(n, v, false);
   if (rc) { n->st = saved; return rc; }
-  k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, c->hist[0], c->hist[1], c->bdt, nm,
-                                                                         n->buf.in0);
+  k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, c->hist[0], c->hist[1], c->bdt,
+                                                                         c->r_hist, nm, n->buf.in0);
   forward(n);
-  k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, n->buf.out, c->cell, nm.s1, c->pc);
+  k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, n->buf.out, c->cell, c->hist[0],
+                                                                        c->hist[1], nm.s1, c->pc);
   n->st = saved;
   c->launches += 18;
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
@@ -357,7 +405,7 @@ int ib3d_net_create(ib3d_net** out, uint64_t seed) {
   for (float** q : fb) ok = ok && cudaMalloc(q, n->nparam * sizeof(float)) == cudaSuccess;
   ok = ok && cudaMalloc(&n->wf, n->nparam * sizeof(bf16)) == cudaSuccess &&
        cudaMalloc(&n->wt, n->nparam * sizeof(bf16)) == cudaSuccess &&
-       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, 4 * sizeof(double)) == cudaSuccess;
+       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, 5 * sizeof(double)) == cudaSuccess;
   if (!ok) {
     ib3d_net_destroy(n);
     return IB3D_ERR_MEMORY;
@@ -403,7 +451,7 @@ int ib3d_net_set_params(ib3d_net* n, const float* in) {
   return IB3D_OK;
 }
 
-// Loss and parameter gradient of one batch given on the host (x: [B][S^3][3] FP32,
+// Loss and parameter gradient of one batch given on the host (x: [B][S^3][kInputs] FP32,
 // target: [B][S^3]); no update. out (may be NULL) receives the network output.
 int ib3d_net_loss_grad(ib3d_net* n, int B, int S, const float* x, const float* target, double* loss, float* grad,
                        float* out) {
@@ -413,8 +461,8 @@ int ib3d_net_loss_grad(ib3d_net* n, int B, int S, const float* x, const float* t
   if (rc) return rc;
   const long long M = v.voxels();
   float* dx = nullptr;
-  NET_CUDA(n, cudaMalloc(&dx, (size_t)M * 3 * sizeof(float)));
-  cudaMemcpyAsync(dx, x, (size_t)M * 3 * sizeof(float), cudaMemcpyHostToDevice, n->st);
+  NET_CUDA(n, cudaMalloc(&dx, (size_t)M * kInputs * sizeof(float)));
+  cudaMemcpyAsync(dx, x, (size_t)M * kInputs * sizeof(float), cudaMemcpyHostToDevice, n->st);
   cudaMemcpyAsync(n->buf.tgt, target, (size_t)M * sizeof(float), cudaMemcpyHostToDevice, n->st);
   k_set_input<<<(unsigned)((M + 255) / 256), 256, 0, n->st>>>(M, dx, n->buf.in0);
   cudaMemsetAsync(n->g, 0, n->nparam * sizeof(float), n->st);
@@ -439,7 +487,7 @@ int ib3d_net_dataset_reserve(ib3d_net* n, int S, int64_t capacity) {
   n->ds_in = nullptr;
   n->ds_t = nullptr;
   const size_t per = (size_t)S * S * S;
-  NET_CUDA(n, cudaMalloc(&n->ds_in, (size_t)capacity * per * 4 * sizeof(bf16)));
+  NET_CUDA(n, cudaMalloc(&n->ds_in, (size_t)capacity * per * kInputs * sizeof(bf16)));
   NET_CUDA(n, cudaMalloc(&n->ds_t, (size_t)capacity * per * sizeof(float)));
   n->S = S;
   n->cap = capacity;
@@ -465,7 +513,8 @@ int ib3d_net_capture(ib3d_net* n, ib3d_ctx* c, int npatches, uint64_t seed) {
     const int j0 = 2 + (int)(rng() % (uint64_t)(c->d.ny - S + 1));
     const int k0 = 2 + (int)(rng() % (uint64_t)(c->d.nz - S + 1));
     k_capture<<<(unsigned)((per + 255) / 256), 256, 0, c->st>>>(c->d, S, i0, j0, k0, c->hist[0], c->hist[1], c->bdt,
-                                                                c->pc, nm, n->ds_in + n->count * per * 4,
+                                                                c->r_hist, c->pc, c->cell, nm,
+                                                                n->ds_in + n->count * per * kInputs,
                                                                 n->ds_t + n->count * per);
     n->count++;
   }

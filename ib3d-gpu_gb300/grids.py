@@ -88,6 +88,102 @@ def tanh_axis(n: int, length: float = 1.0, beta: float = 3.0) -> np.ndarray:
     return np.concatenate([[0.0], np.cumsum(w)])
 
 
+def neumann_coefficients(nodes: np.ndarray) -> np.ndarray:
+    """(n,3) Poisson coefficients of one axis, as coefficientMatrix builds them
+    (subCoefficientMatrix.f90:8-33: pressure-node spacings r1, r2 and
+    2/(r1 rs), -2/(r1 r2), 2/(r2 rs)), with Neumann rows folded in at both ends
+    (A2 += A1 at the first row, A2 += A3 at the last). nodes: the n+1 cell faces."""
+    n = len(nodes) - 1
+    x1 = np.zeros(n + 4)
+    x1[2:n + 3] = nodes
+    d = np.zeros(n + 3)
+    d[2:n + 2] = x1[3:n + 3] - x1[2:n + 2]
+    d[1], d[n + 2] = d[2], d[n + 1]
+    x1[1] = x1[2] - d[1]
+    x1[n + 3] = x1[n + 2] + d[n + 2]
+    xp = np.zeros(n + 3)
+    xp[1:n + 3] = 0.5 * (x1[1:n + 3] + x1[2:n + 4])
+    a = np.zeros((n, 3))
+    i = np.arange(2, n + 2)
+    r1, r2 = xp[i] - xp[i - 1], xp[i + 1] - xp[i]
+    rs = r1 + r2
+    a[:, 0], a[:, 1], a[:, 2] = 2.0 / (r1 * rs), -2.0 / (r1 * r2), 2.0 / (r2 * rs)
+    a[0, 1] += a[0, 0]
+    a[0, 0] = 0.0
+    a[n - 1, 1] += a[n - 1, 2]
+    a[n - 1, 2] = 0.0
+    return a
+
+
+def random_face_velocities(n: tuple, seed: int = 0, passes: int = 3):
+    """Seeded face velocities (ut, vt, wt) in the padded (nx+2, ny+2, nz+2) layout:
+    i.i.d. N(0,1), `passes` passes of a separable [1,1,1]/3 box filter (periodic
+    wrap), mean removed, and zero normal velocity on the six boundary faces so that
+    the divergence is compatible with Neumann conditions."""
+    shape = (n[0] + 2, n[1] + 2, n[2] + 2)
+    rng = np.random.default_rng(seed)
+    out = []
+    for comp in range(3):
+        a = rng.standard_normal(shape)
+        for _ in range(passes):
+            for ax in range(3):
+                a = (np.roll(a, 1, ax) + a + np.roll(a, -1, ax)) / 3.0
+        a -= a.mean()
+        idx = [slice(None)] * 3
+        for face in (0, n[comp]):        # u(1,:,:) and u(nx+1,:,:) (1-based) are the boundary faces
+            idx[comp] = face
+            a[tuple(idx)] = 0.0
+        out.append(np.asfortranarray(a))
+    return tuple(out)
+
+
+def _pressure_nodes(nodes: np.ndarray) -> np.ndarray:
+    """xp(1..n+2) of one axis (1-based, entry 0 unused), with the ghost cells the
+    reference adds (subReadInput.f90:61-68, 119-123)."""
+    n = len(nodes) - 1
+    x1 = np.zeros(n + 4)
+    x1[2:n + 3] = nodes
+    x1[1] = x1[2] - (x1[3] - x1[2])
+    x1[n + 3] = x1[n + 2] + (x1[n + 2] - x1[n + 1])
+    xp = np.zeros(n + 3)
+    xp[1:n + 3] = 0.5 * (x1[1:n + 3] + x1[2:n + 4])
+    return xp
+
+
+def divergence_rhs(x: np.ndarray, y: np.ndarray, z: np.ndarray, faces) -> np.ndarray:
+    """b = div(ut, vt, wt) at every interior cell (computeDiv, subPcorVcor.f90:91-99),
+    made solvable for all-Neumann coefficients: A is not symmetric, and its left null
+    vector is w = wx (x) wy (x) wz with w(i) = (xp(i+1) - xp(i-1))/2 per axis (the row
+    scaling that makes A symmetric), so the w-weighted mean of b is removed."""
+    ut, vt, wt = faces
+    n = (len(x) - 1, len(y) - 1, len(z) - 1)
+    d = [np.diff(a) for a in (x, y, z)]
+    b = np.zeros((n[0] + 2, n[1] + 2, n[2] + 2), order="F")
+    s = np.s_[1:n[0] + 1, 1:n[1] + 1, 1:n[2] + 1]
+    b[s] = ((ut[1:n[0] + 1, 1:n[1] + 1, 1:n[2] + 1] - ut[0:n[0], 1:n[1] + 1, 1:n[2] + 1]) / d[0][:, None, None]
+            + (vt[1:n[0] + 1, 1:n[1] + 1, 1:n[2] + 1] - vt[1:n[0] + 1, 0:n[1], 1:n[2] + 1]) / d[1][None, :, None]
+            + (wt[1:n[0] + 1, 1:n[1] + 1, 1:n[2] + 1] - wt[1:n[0] + 1, 1:n[1] + 1, 0:n[2]]) / d[2][None, None, :])
+    w = []
+    for a in (x, y, z):
+        xp = _pressure_nodes(a)
+        m = len(a) - 1
+        w.append(0.5 * (xp[3:m + 3] - xp[1:m + 1]))
+    W = w[0][:, None, None] * w[1][None, :, None] * w[2][None, None, :]
+    b[s] -= (W * b[s]).sum() / W.sum()
+    return b
+
+
+def poisson_problem(n: int = 256, seed: int = 0):
+    """Standalone pressure-Poisson problem on an n^3 tanh-clustered unit cube:
+    (x, y, z) faces, all-Neumann (acx, acy, acz), the seeded face velocities and the
+    solvable right-hand side b made from their divergence."""
+    x = tanh_axis(n)
+    a = neumann_coefficients(x)
+    faces = random_face_velocities((n, n, n), seed)
+    return {"x": x, "y": x.copy(), "z": x.copy(), "acoef": (a, a.copy(), a.copy()), "faces": faces,
+            "b": divergence_rhs(x, x, x, faces)}
+
+
 # ------------------------------------------------------------------ body
 
 _ICO_FACES = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),

@@ -54,6 +54,10 @@ extern "C" {
 #define IB3D_WARM_PREV 1     /* pc = previous step's pc (linear extrapolation of p) */
 #define IB3D_WARM_LEARNED 2  /* pc = prediction of the attached network (ib3d_attach_net) */
 
+/* ib3d_params.inner_schedule */
+#define IB3D_INNER_FIXED 0
+#define IB3D_INNER_ADAPTIVE 1
+
 typedef struct ib3d_params {
   double re;            /* Reynolds number (inputdata line 2; rev = 1/re, subReadInput.f90:22) */
   double deltat;        /* time step (subReadInput.f90:24) */
@@ -69,6 +73,11 @@ typedef struct ib3d_params {
   double omega_inner;   /* relaxation factor of the FP32 inner sweeps (0: use omega). The FP64
                            defect correction fixes the final accuracy, so the inner solve may use
                            its own factor. */
+  int32_t inner_schedule; /* IB3D_INNER_FIXED: every pass runs inner_sweeps; IB3D_INNER_ADAPTIVE:
+                             the first pass runs inner_sweeps, later passes as many as the measured
+                             residual reduction per sweep predicts are needed to reach eps (at most
+                             four decades per FP32 solve), so fewer FP64 residual passes run and the
+                             last pass overshoots less */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
@@ -79,6 +88,7 @@ typedef struct ib3d_solve_stats {
   double derr_std_st;    /* max |u_new - u_old| / dt over fluid cells */
   double final_err;      /* last value of the stopping test */
   double solve_seconds;  /* device time of the SOR loop (cpu_time pair at :33,:37) */
+  double initial_err;    /* IB3D_PREC_FP32DC: FP64 residual L-inf of the initial guess */
 } ib3d_solve_stats;
 
 typedef struct ib3d_ctx ib3d_ctx;
@@ -103,6 +113,27 @@ int ib3d_set_params(ib3d_ctx* ctx, const ib3d_params* prm);
 int ib3d_set_mesh(ib3d_ctx* ctx, int64_t nnodes, const double* xn, const double* yn, const double* zn,
                   int64_t nelems, const int64_t* e1, const int64_t* e2, const int64_t* e3,
                   double xshift, double yshift, double zshift, int64_t inor);
+
+/* Replaces the Poisson coefficient tables that ib3d_create builds as
+ * coefficientMatrix does (subCoefficientMatrix.f90:1-59: the 1-D three-point
+ * coefficients with the inlet/wall Neumann and outlet Dirichlet rows folded in).
+ * acx is (nx,3) column-major like Acx (acy, acz likewise), for boundary conditions
+ * the reference does not fold in, e.g. Neumann on all six faces. Both the FP64
+ * tables and the FP32 copies of the mixed-precision solve are replaced. */
+int ib3d_set_poisson_coefficients(ib3d_ctx* ctx, const double* acx, const double* acy, const double* acz);
+
+/* Prescribed body motion (replaces shiftSurfaceNodesMovingbody, subSearch.f90:41-76,
+ * whose shift is integrated from the force; here the caller gives it). Shifts every
+ * surface node by (dx, dy, dz) (xnode1 = xr + xmove, :64-73), recomputes the
+ * surface normals (computeSurfaceNorm, :80-131), and makes (us, vs, ws) the
+ * surface velocity of the velocity forcing (the reference's commented hooks
+ * usurf = u_curr etc., subForcing.f90:144, 228, 312, 397, 482, 566) and, with the
+ * previous call's velocity, the acceleration in the pressure forcing's
+ * dpdn = (-(v_curr - v_prev)/deltat)*cosBeta (hook at :20, summed over the three
+ * axes). The search results describe the old position afterwards: call
+ * ib3d_search before the next forcing. A context never moved keeps the reference's
+ * fixed-body forcing (surface velocity 0, dpdn = 0). */
+int ib3d_move_body(ib3d_ctx* ctx, double dx, double dy, double dz, double us, double vs, double ws);
 
 /* tagging (subSearch.f90:134-321), cellCount (subSearch.f90:515-596) and
  * computeNormDistance (subSearch.f90:599-678), plus the ghost-point schedule.
@@ -138,6 +169,12 @@ int ib3d_pressure_forcing(ib3d_ctx* ctx); /* pressureForcing1, subForcing.f90:2-
 /* poissonSolver, subPcorVcor.f90:2-80 (computeDiv, REDBLACKSOR, correctPressure,
  * correctVelocity, velocityBC, steady-state indicator, u = ut). stats may be NULL. */
 int ib3d_poisson_solver(ib3d_ctx* ctx, ib3d_solve_stats* stats);
+/* REDBLACKSOR alone (subPcorVcor.f90:148-212): solves A pc = b/deltat on the fluid
+ * cells for the b already in the context (ib3d_set_field field 8), with the
+ * context's precision, stopping test and warm start (IB3D_WARM_ZERO starts from
+ * pc = 0 as poissonSolver does, :19-28); no divergence and no corrections. */
+int ib3d_redblack_sor(ib3d_ctx* ctx, ib3d_solve_stats* stats);
+
 /* stressCal1 (first != 0, subStressCal1.f90:2-460) or stressCal2 (subStressCal2.f90:2-381):
  * coef = {Cd viscous, Cd pressure, Cl viscous, Cl pressure} (dragcoff.dat / liftcoff.dat). */
 int ib3d_stress(ib3d_ctx* ctx, int first, double coef[4]);
@@ -171,13 +208,16 @@ void* ib3d_device_field(ib3d_ctx* ctx, int which);
 /* Blocks until the context's stream is idle. */
 int ib3d_synchronize(ib3d_ctx* ctx);
 
-/* ---- Learned warm start (no counterpart in the reference; configs[3]) --------------
+/* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A 3-level 3-D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
- * activations, FP32 accumulation) predicts each step's pressure correction pc from
- * the two previous pressures and the step's b/dt; the prediction is the SOR initial
- * guess and the FP64 stopping test is unchanged. It is trained on the GPU by this
- * library's own forward, backward and Adam kernels on patches captured from solver
- * runs. */
+ * activations, FP32 accumulation) predicts the change of the pressure correction
+ * from one step to the next, pc^n - pc^{n-1}, from four inputs per cell: the
+ * previous correction (p^{n-1} - p^{n-2}), b/dt, p^{n-1}, and the FP64 residual of
+ * the previous correction against this step's b/dt divided by the diagonal of A.
+ * pc^{n-1} plus the prediction is the SOR initial guess; the FP64 stopping test is
+ * unchanged, so the previous correction (IB3D_WARM_PREV) is both the fallback and
+ * the yardstick. The network is trained on the GPU by this library's own forward,
+ * backward and Adam kernels on patches captured from solver runs. */
 typedef struct ib3d_net ib3d_net;
 int ib3d_net_create(ib3d_net** out, uint64_t seed);   /* He-initialised weights */
 void ib3d_net_destroy(ib3d_net* net);
@@ -186,7 +226,8 @@ int64_t ib3d_net_num_params(const ib3d_net* net);
 int ib3d_net_get_params(ib3d_net* net, float* out);
 int ib3d_net_set_params(ib3d_net* net, const float* in);
 /* Loss (mean squared error) and gradient of one batch given on the host: x is
- * [B][S^3][3] FP32 (x fastest within a patch), target [B][S^3]; S a multiple of 4.
+ * [B][S^3][4] FP32 (the four inputs above, x fastest within a patch), target
+ * [B][S^3]; S a multiple of 4.
  * out (may be NULL) receives the prediction. No parameter update. */
 int ib3d_net_loss_grad(ib3d_net* net, int B, int S, const float* x, const float* target, double* loss, float* grad,
                        float* out);
@@ -197,8 +238,8 @@ int ib3d_net_dataset_reserve(ib3d_net* net, int S, int64_t capacity);
 int64_t ib3d_net_dataset_size(const ib3d_net* net);
 int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
 int ib3d_net_train(ib3d_net* net, int steps, int batch, double lr, uint64_t seed, double* last_loss);
-/* Keeps the two previous pressures in ctx (needed by capture and by the learned
- * warm start); ib3d_attach_net calls it. */
+/* Keeps the two previous pressures and the previous correction's residual in ctx
+ * (needed by capture and by the learned warm start); ib3d_attach_net calls it. */
 int ib3d_enable_history(ib3d_ctx* ctx);
 /* Network used by IB3D_WARM_LEARNED (NULL detaches). */
 int ib3d_attach_net(ib3d_ctx* ctx, ib3d_net* net);

@@ -36,6 +36,9 @@ struct OrState {
   double *xnode1, *ynode1, *znode1;
   int64_t *e1, *e2, *e3;
   double *xcent, *ycent, *zcent, *cosA, *cosB, *cosG, *alpha3, *beta3, *gamma3;
+  /* body motion: surface velocity now and one step earlier (0 for a fixed body) */
+  int moving;
+  double bvel[3], bprev[3];
   /* cell lists, (n,3) col-major, 1-based rows */
   int64_t nfluid, nsolid, nib, nred, nblack;
   int64_t *fluid, *solid, *ib, *red, *black;
@@ -151,6 +154,29 @@ void or_destroy(OrState* s) {
   free(s);
 }
 
+/* computeSurfaceNorm (subSearch.f90:80-131): centroids, cross-product normals,
+ * unit normals times inor. */
+static void surface_norm(OrState* s) {
+  const int64_t nelems = s->nelems;
+  const double dinor = (double)s->inor;
+  for (int64_t n = 1; n <= nelems; ++n) {      /* subSearch.f90:95-125 */
+    double p1x = s->xnode1[s->e1[n]], p1y = s->ynode1[s->e1[n]], p1z = s->znode1[s->e1[n]];
+    double p2x = s->xnode1[s->e2[n]], p2y = s->ynode1[s->e2[n]], p2z = s->znode1[s->e2[n]];
+    double p3x = s->xnode1[s->e3[n]], p3y = s->ynode1[s->e3[n]], p3z = s->znode1[s->e3[n]];
+    s->xcent[n] = ((p2x + p1x) + p3x) / 3.0;
+    s->ycent[n] = ((p2y + p1y) + p3y) / 3.0;
+    s->zcent[n] = ((p2z + p1z) + p3z) / 3.0;
+    double ca = (p2y - p1y) * (p3z - p1z) - (p3y - p1y) * (p2z - p1z);
+    double cb = (p2z - p1z) * (p3x - p1x) - (p3z - p1z) * (p2x - p1x);
+    double cg = (p2x - p1x) * (p3y - p1y) - (p3x - p1x) * (p2y - p1y);
+    s->alpha3[n] = ca; s->beta3[n] = cb; s->gamma3[n] = cg;
+    double len = sqrt((SQ(ca) + SQ(cb)) + SQ(cg));
+    s->cosA[n] = (ca / len) * dinor;
+    s->cosB[n] = (cb / len) * dinor;
+    s->cosG[n] = (cg / len) * dinor;
+  }
+}
+
 /* shiftSurfaceNodesInitial (subSearch.f90:2-39) + computeSurfaceNorm (80-131). */
 int or_set_mesh(OrState* s, int64_t nnodes, const double* xn, const double* yn, const double* zn,
                 int64_t nelems, const int64_t* e1, const int64_t* e2, const int64_t* e3,
@@ -172,29 +198,100 @@ int or_set_mesh(OrState* s, int64_t nnodes, const double* xn, const double* yn, 
   for (int64_t n = 1; n <= nelems; ++n) { s->e1[n] = e1[n - 1]; s->e2[n] = e2[n - 1]; s->e3[n] = e3[n - 1]; }
   double** a[] = {&s->xcent, &s->ycent, &s->zcent, &s->cosA, &s->cosB, &s->cosG, &s->alpha3, &s->beta3, &s->gamma3};
   for (int q = 0; q < 9; ++q) *a[q] = alloc1(nelems);
-  const double dinor = (double)inor;
-  for (int64_t n = 1; n <= nelems; ++n) {      /* subSearch.f90:95-125 */
-    double p1x = s->xnode1[s->e1[n]], p1y = s->ynode1[s->e1[n]], p1z = s->znode1[s->e1[n]];
-    double p2x = s->xnode1[s->e2[n]], p2y = s->ynode1[s->e2[n]], p2z = s->znode1[s->e2[n]];
-    double p3x = s->xnode1[s->e3[n]], p3y = s->ynode1[s->e3[n]], p3z = s->znode1[s->e3[n]];
-    s->xcent[n] = ((p2x + p1x) + p3x) / 3.0;
-    s->ycent[n] = ((p2y + p1y) + p3y) / 3.0;
-    s->zcent[n] = ((p2z + p1z) + p3z) / 3.0;
-    double ca = (p2y - p1y) * (p3z - p1z) - (p3y - p1y) * (p2z - p1z);
-    double cb = (p2z - p1z) * (p3x - p1x) - (p3z - p1z) * (p2x - p1x);
-    double cg = (p2x - p1x) * (p3y - p1y) - (p3x - p1x) * (p2y - p1y);
-    s->alpha3[n] = ca; s->beta3[n] = cb; s->gamma3[n] = cg;
-    double len = sqrt((SQ(ca) + SQ(cb)) + SQ(cg));
-    s->cosA[n] = (ca / len) * dinor;
-    s->cosB[n] = (cb / len) * dinor;
-    s->cosG[n] = (cg / len) * dinor;
-  }
+  surface_norm(s);
   return 0;
+}
+
+/* Prescribed body motion: the node shift of shiftSurfaceNodesMovingbody
+ * (subSearch.f90:64-73, xnode1 = xr + xmove) with (xmove, ymove, zmove) given
+ * instead of integrated from the force, then computeSurfaceNorm again. (us, vs, ws)
+ * becomes the surface velocity of the velocity forcing (the commented hooks
+ * usurf = u_curr etc., subForcing.f90:144, 228, 312, 397, 482, 566) and, with the
+ * previous call's velocity, the body acceleration in dpdn (hook at :20). The
+ * search must be run again before the next forcing. */
+int or_move_body(OrState* s, double dx, double dy, double dz, double us, double vs, double ws) {
+  if (!s->xnode1) return -2;
+  for (int64_t i = 1; i <= s->nnodes; ++i) {
+    const double xr = s->xnode1[i], yr = s->ynode1[i], zr = s->znode1[i];
+    s->xnode1[i] = xr + dx;
+    s->ynode1[i] = yr + dy;
+    s->znode1[i] = zr + dz;
+  }
+  surface_norm(s);
+  if (s->moving) {
+    s->bprev[0] = s->bvel[0]; s->bprev[1] = s->bvel[1]; s->bprev[2] = s->bvel[2];
+  } else {
+    s->bprev[0] = us; s->bprev[1] = vs; s->bprev[2] = ws;   /* no acceleration on the first move */
+  }
+  s->bvel[0] = us; s->bvel[1] = vs; s->bvel[2] = ws;
+  s->moving = 1;
+  s->have_scache = 0;
+  return 0;
+}
+
+/* Replaces the tables coefficientMatrix built (subCoefficientMatrix.f90:1-59), for
+ * boundary conditions the reference does not fold in (all-Neumann, say); each
+ * array is (n,3) column-major like Acx. */
+void or_set_coefficients(OrState* s, const double* acx, const double* acy, const double* acz) {
+  memcpy(s->Acx, acx, (size_t)(3 * s->nx) * sizeof(double));
+  memcpy(s->Acy, acy, (size_t)(3 * s->ny) * sizeof(double));
+  memcpy(s->Acz, acz, (size_t)(3 * s->nz) * sizeof(double));
 }
 
 /* Signed distance of a corner to the plane of element m (subSearch.f90:204-234). */
 static inline double corner_dot(const OrState* s, int64_t m, double x, double y, double z) {
   return ((x - s->xcent[m]) * s->cosA[m] + (y - s->ycent[m]) * s->cosB[m]) + (z - s->zcent[m]) * s->cosG[m];
+}
+
+/* cellCount (subSearch.f90:515-596): lexicographic compaction of the flags into the
+ * fluid, solid and IB lists, and the fluid list into red and black. */
+static void cell_count(OrState* s) {
+  const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
+  int64_t nf = 0, ns = 0, nb = 0;
+  for (int64_t k = 2; k <= nz + 1; ++k)
+    for (int64_t j = 2; j <= ny + 1; ++j)
+      for (int64_t i = 2; i <= nx + 1; ++i) {
+        int64_t c = F3(s->cell, i, j, k);
+        if (c == 0) ++nf; else if (c == 1) ++ns; else if (c == 2) ++nb;
+      }
+  free(s->fluid); free(s->solid); free(s->ib); free(s->red); free(s->black);
+  s->nfluid = nf; s->nsolid = ns; s->nib = nb;
+  s->fluid = (int64_t*)malloc((size_t)(3 * nf + 3) * sizeof(int64_t));
+  s->solid = (int64_t*)malloc((size_t)(3 * ns + 3) * sizeof(int64_t));
+  s->ib = (int64_t*)malloc((size_t)(3 * nb + 3) * sizeof(int64_t));
+  int64_t a = 0, bq = 0, c2 = 0;
+  for (int64_t k = 2; k <= nz + 1; ++k)
+    for (int64_t j = 2; j <= ny + 1; ++j)
+      for (int64_t i = 2; i <= nx + 1; ++i) {
+        int64_t c = F3(s->cell, i, j, k);
+        if (c == 0) { ++a; L(s->fluid, nf, a, 1) = i; L(s->fluid, nf, a, 2) = j; L(s->fluid, nf, a, 3) = k; }
+        else if (c == 1) { ++bq; L(s->solid, ns, bq, 1) = i; L(s->solid, ns, bq, 2) = j; L(s->solid, ns, bq, 3) = k; }
+        else if (c == 2) { ++c2; L(s->ib, nb, c2, 1) = i; L(s->ib, nb, c2, 2) = j; L(s->ib, nb, c2, 3) = k; }
+      }
+  int64_t nr = 0, nk = 0;
+  for (int64_t n = 1; n <= nf; ++n) {
+    int64_t sum = L(s->fluid, nf, n, 1) + L(s->fluid, nf, n, 2) + L(s->fluid, nf, n, 3);
+    if (sum % 2 == 1) ++nr; else ++nk;                      /* :562 */
+  }
+  s->nred = nr; s->nblack = nk;
+  s->red = (int64_t*)malloc((size_t)(3 * nr + 3) * sizeof(int64_t));
+  s->black = (int64_t*)malloc((size_t)(3 * nk + 3) * sizeof(int64_t));
+  int64_t ir = 0, ik = 0;
+  for (int64_t n = 1; n <= nf; ++n) {
+    int64_t i = L(s->fluid, nf, n, 1), j = L(s->fluid, nf, n, 2), k = L(s->fluid, nf, n, 3);
+    if ((i + j + k) % 2 == 1) { ++ir; L(s->red, nr, ir, 1) = i; L(s->red, nr, ir, 2) = j; L(s->red, nr, ir, 3) = k; }
+    else { ++ik; L(s->black, nk, ik, 1) = i; L(s->black, nk, ik, 2) = j; L(s->black, nk, ik, 3) = k; }
+  }
+}
+
+/* No body: every interior cell fluid (the flags tagging leaves outside its box). */
+void or_no_body(OrState* s) {
+  const int64_t n3 = NX2 * NY2 * (s->nz + 2);
+  memset(s->cell, 0, (size_t)n3 * sizeof(int64_t));
+  cell_count(s);
+  for (int q = 0; q < 7; ++q) { free(s->nd[q]); s->nd[q] = alloc1(0); }
+  free(s->nelp);
+  s->nelp = (int64_t*)calloc(1, sizeof(int64_t));
 }
 
 /* tagging (subSearch.f90:134-321), cellCount (515-596), computeNormDistance (599-678). */
@@ -237,42 +334,8 @@ int or_search(OrState* s, const int64_t box[6]) {
         }
         F3(s->cell, i, j, k) = all_in ? 1 : (all_out ? 0 : 2);   /* :238-247 */
       }
-  /* cellCount: lexicographic compaction (subSearch.f90:532-589). */
-  int64_t nf = 0, ns = 0, nb = 0;
-  for (int64_t k = 2; k <= nz + 1; ++k)
-    for (int64_t j = 2; j <= ny + 1; ++j)
-      for (int64_t i = 2; i <= nx + 1; ++i) {
-        int64_t c = F3(s->cell, i, j, k);
-        if (c == 0) ++nf; else if (c == 1) ++ns; else if (c == 2) ++nb;
-      }
-  free(s->fluid); free(s->solid); free(s->ib); free(s->red); free(s->black);
-  s->nfluid = nf; s->nsolid = ns; s->nib = nb;
-  s->fluid = (int64_t*)malloc((size_t)(3 * nf + 3) * sizeof(int64_t));
-  s->solid = (int64_t*)malloc((size_t)(3 * ns + 3) * sizeof(int64_t));
-  s->ib = (int64_t*)malloc((size_t)(3 * nb + 3) * sizeof(int64_t));
-  int64_t a = 0, bq = 0, c2 = 0;
-  for (int64_t k = 2; k <= nz + 1; ++k)
-    for (int64_t j = 2; j <= ny + 1; ++j)
-      for (int64_t i = 2; i <= nx + 1; ++i) {
-        int64_t c = F3(s->cell, i, j, k);
-        if (c == 0) { ++a; L(s->fluid, nf, a, 1) = i; L(s->fluid, nf, a, 2) = j; L(s->fluid, nf, a, 3) = k; }
-        else if (c == 1) { ++bq; L(s->solid, ns, bq, 1) = i; L(s->solid, ns, bq, 2) = j; L(s->solid, ns, bq, 3) = k; }
-        else if (c == 2) { ++c2; L(s->ib, nb, c2, 1) = i; L(s->ib, nb, c2, 2) = j; L(s->ib, nb, c2, 3) = k; }
-      }
-  int64_t nr = 0, nk = 0;
-  for (int64_t n = 1; n <= nf; ++n) {
-    int64_t sum = L(s->fluid, nf, n, 1) + L(s->fluid, nf, n, 2) + L(s->fluid, nf, n, 3);
-    if (sum % 2 == 1) ++nr; else ++nk;                      /* :562 */
-  }
-  s->nred = nr; s->nblack = nk;
-  s->red = (int64_t*)malloc((size_t)(3 * nr + 3) * sizeof(int64_t));
-  s->black = (int64_t*)malloc((size_t)(3 * nk + 3) * sizeof(int64_t));
-  int64_t ir = 0, ik = 0;
-  for (int64_t n = 1; n <= nf; ++n) {
-    int64_t i = L(s->fluid, nf, n, 1), j = L(s->fluid, nf, n, 2), k = L(s->fluid, nf, n, 3);
-    if ((i + j + k) % 2 == 1) { ++ir; L(s->red, nr, ir, 1) = i; L(s->red, nr, ir, 2) = j; L(s->red, nr, ir, 3) = k; }
-    else { ++ik; L(s->black, nk, ik, 1) = i; L(s->black, nk, ik, 2) = j; L(s->black, nk, ik, 3) = k; }
-  }
+  cell_count(s);
+  const int64_t nb = s->nib;
   /* computeNormDistance (subSearch.f90:621-672). */
   for (int q = 0; q < 7; ++q) { free(s->nd[q]); s->nd[q] = alloc1(nb); }
   free(s->nelp);
@@ -696,7 +759,7 @@ int or_velocity_forcing(OrState* s) {
       const double* Y = g->field == 0 ? s->yu : g->field == 1 ? s->yv : s->yw;
       const double* Z = g->field == 0 ? s->zu : g->field == 1 ? s->zv : s->zw;
       const double* A3[3] = {X, Y, Z};
-      const double surf = 0.0;
+      const double surf = s->moving ? s->bvel[g->field] : 0.0;   /* usurf = u_curr (:144) */
       const double sd = s->nd[g->nd][n];
       const double pt1 = 1.5 * diag + (fabs(sd) - sd) * 0.5;
       const double pos[3] = {X[i + g->node_off[0]] + pt1 * s->cosA[nel],
@@ -724,13 +787,17 @@ int or_velocity_forcing(OrState* s) {
   return 0;
 }
 
-/* pressureForcing1 (subForcing.f90:2-103), dpdn = 0 for a fixed body (:11). */
+/* pressureForcing1 (subForcing.f90:2-103). dpdn = 0 for a fixed body (:11); for a
+ * moving one the hook at :20, dpdn = (-(v_curr-v_prev)/deltat)*cosBeta(nelp(n)),
+ * summed over the three axes in x, y, z order. */
 int or_pressure_forcing(OrState* s) {
   const int64_t nx = s->nx, ny = s->ny, nz = s->nz, nb = s->nib;
-  const double dpdn = 0.0;
+  const double acc[3] = {-(s->bvel[0] - s->bprev[0]) / s->deltat, -(s->bvel[1] - s->bprev[1]) / s->deltat,
+                         -(s->bvel[2] - s->bprev[2]) / s->deltat};
   for (int64_t n = 1; n <= nb; ++n) {
     const int64_t i = L(s->ib, nb, n, 1), j = L(s->ib, nb, n, 2), k = L(s->ib, nb, n, 3);
     const int64_t nel = s->nelp[n];
+    const double dpdn = s->moving ? (acc[0] * s->cosA[nel] + acc[1] * s->cosB[nel]) + acc[2] * s->cosG[nel] : 0.0;
     const double sd = s->nd[0][n];
     const double pt1 = 1.5 * sqrt((SQ(s->deltax[i]) + SQ(s->deltay[j])) + SQ(s->deltaz[k])) + (fabs(sd) - sd) * 0.5;
     const double px = s->xp[i] + pt1 * s->cosA[nel];
@@ -827,6 +894,20 @@ static int red_black_sor(OrState* s, int64_t* isum_out, double* err_out) {
 /* poissonSolver (subPcorVcor.f90:2-80) with computeDiv (82-101), correctPressure
  * (105-120), correctVelocity (125-142), velocityBC and the steady-state
  * indicator (45-58). */
+/* REDBLACKSOR alone (subPcorVcor.f90:148-212) on the b already in place, from pc = 0
+ * as poissonSolver starts it (:19-28); no divergence, no corrections. */
+int or_redblack_sor(OrState* s, int64_t* nsweeps, double* final_err) {
+  const int64_t n3 = NX2 * NY2 * (s->nz + 2);
+  memset(s->pc, 0, (size_t)n3 * sizeof(double));
+  memset(s->pco, 0, (size_t)n3 * sizeof(double));
+  int64_t isum = 0;
+  double err = 0.0;
+  const int rc = red_black_sor(s, &isum, &err);
+  if (nsweeps) *nsweeps = isum;
+  if (final_err) *final_err = err;
+  return rc;
+}
+
 int or_poisson_solver(OrState* s, int64_t* nsweeps, double* divmax_out, double* derrStdSt_out,
                       double* final_err) {
   const int64_t n3 = NX2 * NY2 * (s->nz + 2);

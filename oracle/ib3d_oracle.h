@@ -46,14 +46,26 @@ int or_set_mesh(OrState* s, int64_t nnodes, const double* xn, const double* yn, 
                 int64_t nelems, const int64_t* e1, const int64_t* e2, const int64_t* e3,
                 double xshift, double yshift, double zshift, int64_t inor);
 
+/* Prescribed motion: shift every surface node by (dx, dy, dz) as
+ * shiftSurfaceNodesMovingbody does (subSearch.f90:64-73), recompute the surface
+ * normals (80-131), and make (us, vs, ws) the surface velocity of the forcing
+ * (usurf/vsurf/wsurf, subForcing.f90:144-145 etc.) and of dpdn (:20). Call
+ * or_search afterwards. */
+int or_move_body(OrState* s, double dx, double dy, double dz, double us, double vs, double ws);
+
 /* tagging (subSearch.f90:134-321) + cellCount (515-596) + computeNormDistance (599-678).
  * box = {i_start, i_end, j_start, j_end, k_start, k_end} (1-based, inclusive). */
 int or_search(OrState* s, const int64_t box[6]);
+
+/* No body at all: every interior cell fluid, lists built as cellCount does. */
+void or_no_body(OrState* s);
 
 /* Setup routines run once before the time loop (main.f90:15-18). */
 void or_initial_conditions(OrState* s);   /* subInitialConditions.f90:2-48 */
 void or_coefficient_matrix(OrState* s);   /* subCoefficientMatrix.f90:1-59 */
 void or_non_uni_coeff(OrState* s);        /* subNavierStokes.f90:3-619 */
+/* Replaces the Acx/Acy/Acz tables ((n,3) column-major) after or_coefficient_matrix. */
+void or_set_coefficients(OrState* s, const double* acx, const double* acy, const double* acz);
 
 /* Per-step routines (main.f90:29-39 and 42-66). */
 void or_ns_momentum(OrState* s);                        /* subNavierStokes.f90:622-1122 */
@@ -64,6 +76,9 @@ int or_pressure_forcing(OrState* s);                    /* subForcing.f90:2-103 
 int or_poisson_solver(OrState* s, int64_t* nsweeps, double* divmax, double* derrStdSt,
                       double* final_err);               /* subPcorVcor.f90:2-80 */
 int or_stress(OrState* s, int first, double coef[4]);   /* subStressCal1/2.f90 */
+/* REDBLACKSOR alone (subPcorVcor.f90:148-212) on the b set by the caller (field 8),
+ * pc starting from 0. */
+int or_redblack_sor(OrState* s, int64_t* nsweeps, double* final_err);
 /* One full time step as main.f90:42-66 sequences it; first selects stressCal1. */
 int or_step(OrState* s, int first, int64_t* nsweeps, double coef[4]);
 

@@ -39,8 +39,12 @@ def lib() -> C.CDLL:
         "or_set_mesh": (C.c_int, [_VP, C.c_int64, _D, _D, _D, C.c_int64, _I64, _I64, _I64, C.c_double, C.c_double,
                                   C.c_double, C.c_int64]),
         "or_search": (C.c_int, [_VP, _I64]),
+        "or_move_body": (C.c_int, [_VP] + [C.c_double] * 6),
         "or_initial_conditions": (None, [_VP]),
         "or_coefficient_matrix": (None, [_VP]),
+        "or_set_coefficients": (None, [_VP, _D, _D, _D]),
+        "or_no_body": (None, [_VP]),
+        "or_redblack_sor": (C.c_int, [_VP, _I64, _D]),
         "or_non_uni_coeff": (None, [_VP]),
         "or_ns_momentum": (None, [_VP]),
         "or_velocity_bc": (None, [_VP]),
@@ -128,6 +132,14 @@ class Oracle:
                                      float(shift[1]), float(shift[2]), int(inor)), "or_set_mesh")
         self.nelems = len(tris)
 
+    def no_body(self):
+        """Every interior cell fluid (no surface mesh, no search)."""
+        self.L.or_no_body(self._h)
+        self.counts = {"fluid": self.nx * self.ny * self.nz, "solid": 0, "ib": 0}
+
+    def move_body(self, dx, dy, dz, us=0.0, vs=0.0, ws=0.0):
+        self._chk(self.L.or_move_body(self._h, dx, dy, dz, us, vs, ws), "or_move_body")
+
     def search(self, box) -> dict:
         b = np.asarray(box, dtype=np.int64)
         self._chk(self.L.or_search(self._h, b.ctypes.data_as(_I64)), "or_search")
@@ -161,6 +173,11 @@ class Oracle:
     def acoef(self, axis: int) -> np.ndarray:
         n = (self.nx, self.ny, self.nz)[axis]
         return np.ctypeslib.as_array(self.L.or_acoef(self._h, axis), shape=(3 * n,)).reshape((n, 3), order="F").copy()
+
+    def set_acoef(self, acx, acy, acz):
+        """Replaces Acx/Acy/Acz ((n,3) arrays) for other boundary conditions."""
+        a = [np.asfortranarray(v, dtype=np.float64) for v in (acx, acy, acz)]
+        self.L.or_set_coefficients(self._h, *(v.ctypes.data_as(_D) for v in a))
 
     def conv_coef(self, fam: int, m: int) -> np.ndarray:
         n = (self.nx, self.ny, self.nz)[fam % 3]
@@ -206,6 +223,14 @@ class Oracle:
         if rc and not allow_noconv:
             raise OracleError(rc, "or_poisson_solver")
         return {"sweeps": int(ns[0]), "divmax": vals[0], "derr_std_st": vals[1], "final_err": vals[2], "rc": rc}
+
+    def redblack_sor(self, allow_noconv: bool = False) -> dict:
+        ns = np.zeros(1, np.int64)
+        err = np.zeros(1)
+        rc = self.L.or_redblack_sor(self._h, ns.ctypes.data_as(_I64), err.ctypes.data_as(_D))
+        if rc and not (allow_noconv and rc == 1):
+            raise OracleError(rc, "or_redblack_sor")
+        return {"sweeps": int(ns[0]), "final_err": float(err[0]), "rc": rc}
 
     def stress(self, first: bool) -> np.ndarray:
         coef = np.zeros(4)

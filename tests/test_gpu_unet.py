@@ -46,8 +46,8 @@ def torch_forward(params: np.ndarray, x: np.ndarray, bf16: bool = False):
     st = Stored.apply
     lay, head = layout()
     p = torch.tensor(params.astype(np.float64), requires_grad=True)
-    xt = torch.tensor(x.astype(np.float64)).permute(0, 4, 1, 2, 3)        # B,3,S,S,S
-    xt = rb(torch.cat([xt, torch.zeros(xt.shape[0], 13, *xt.shape[2:], dtype=xt.dtype)], 1))
+    xt = torch.tensor(x.astype(np.float64)).permute(0, 4, 1, 2, 3)        # B,4,S,S,S
+    xt = rb(torch.cat([xt, torch.zeros(xt.shape[0], 16 - xt.shape[1], *xt.shape[2:], dtype=xt.dtype)], 1))
 
     def conv(t, l):
         w, b, n, k = lay[l]
@@ -99,7 +99,7 @@ def test_net_loss_and_gradients_match_float64_reference(ib3d):
     assert net.nparams == head + 17
     rng = np.random.default_rng(1)
     B, S = 2, 8
-    x = rng.standard_normal((B, S, S, S, 3)).astype(np.float32)
+    x = rng.standard_normal((B, S, S, S, 4)).astype(np.float32)
     t = rng.standard_normal((B, S, S, S)).astype(np.float32)
     params = net.get_params()
     params[head:head + 16] = rng.standard_normal(16) * 0.3   # a head large enough to carry gradient
@@ -117,8 +117,9 @@ def test_net_loss_and_gradients_match_float64_reference(ib3d):
 
 
 def test_capture_train_and_learned_warm_start(ib3d, grids):
-    """Patches captured from a small run train the network (the loss falls), and
-    steps warm-started by it still stop at the same FP64 residual with drag/lift
+    """Patches captured from a small run train the network: on the same batches
+    (chosen by seed; lr = 0 evaluates without moving the weights) the loss falls.
+    Steps warm-started by it still stop at the same FP64 residual, with drag/lift
     within 1e-4 of the FP64 path."""
     cs = grids.case("small")
     common = dict(precision=ib3d.PREC_FP32DC, criterion=ib3d.CRIT_RESIDUAL, eps=1e-6, inner_sweeps=64)
@@ -131,10 +132,15 @@ def test_capture_train_and_learned_warm_start(ib3d, grids):
         if step >= 3:
             net.capture(src, 16, seed=step)
     assert net.dataset_size() == 96
-    first = net.train(1, batch=4, lr=1e-3, seed=1)
-    last = net.train(150, batch=4, lr=1e-3, seed=2)
-    print(f"training loss {first:.4f} -> {last:.4f}")
-    assert last < 0.7 * first, (first, last)
+
+    def fit():
+        return float(np.mean([net.train(1, batch=8, lr=0.0, seed=1000 + q) for q in range(8)]))
+
+    before = fit()
+    net.train(300, batch=4, lr=1e-3, seed=2)
+    after = fit()
+    print(f"training-set loss {before:.4f} -> {after:.4f}")
+    assert after < 0.8 * before, (before, after)
     ref = ib3d.setup_case(cs, precision=ib3d.PREC_FP64, criterion=ib3d.CRIT_RESIDUAL, eps=1e-6, check_every=1)
     lrn = ib3d.setup_case(cs, warm_start=ib3d.WARM_LEARNED, **common)
     lrn.attach_net(net)

@@ -157,3 +157,54 @@ def test_sor_noconv_cap(oracle_mod, grids):
     o.ns_momentum(); o.velocity_bc(); o.solid_cell_bc(); o.velocity_forcing(); o.velocity_bc()
     st = o.poisson_solver(allow_noconv=True)
     assert st["rc"] == 1 and st["sweeps"] == 7
+
+
+def test_moved_body_shifts_flags_and_zero_motion_changes_nothing(oracle_mod, grids):
+    """or_move_body: a shift of exactly one core cell in y moves the core flags by one
+    index in j (up to corners that sit on the surface within rounding); a zero shift
+    at zero velocity leaves the search and a whole step unchanged (surface velocity
+    0 and dpdn 0 as for the fixed body)."""
+    cs = grids.case("tiny")
+    h = 1.0 / 8                       # the tiny case's uniform core spacing
+    a = oracle_mod.setup_case(cs)
+    b = oracle_mod.setup_case(cs)
+    b.move_body(0.0, h, 0.0, 0.0, 0.0, 0.0)
+    b.search(cs.box)
+    ca, cb = a.get_search()["cell"], b.get_search()["cell"]
+    assert a.counts["solid"] == b.counts["solid"] or abs(a.counts["solid"] - b.counts["solid"]) <= 2
+    i0, i1, j0, j1, k0, k1 = (int(v) for v in cs.box)
+    core_a = ca[i0:i1, j0:j1 - 1, k0:k1]
+    core_b = cb[i0:i1, j0 + 1:j1, k0:k1]
+    assert np.mean(core_a == core_b) > 0.999
+    c = oracle_mod.setup_case(cs)
+    c.move_body(0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    c.search(cs.box)
+    d = oracle_mod.setup_case(cs)
+    assert np.array_equal(c.get_search()["cell"], d.get_search()["cell"])
+    for step in (1, 2):
+        sc, kc = c.step(step == 1)
+        sd, kd = d.step(step == 1)
+        assert sc["sweeps"] == sd["sweeps"] and np.array_equal(kc, kd)
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(c.get_field(f), d.get_field(f)), f
+
+
+def test_neumann_coefficients_and_standalone_sor(oracle_mod, grids):
+    """grids.neumann_coefficients reproduces coefficientMatrix's interior rows and its
+    Neumann folding, and REDBLACKSOR on the all-Neumann cube with the weighted-mean-free
+    divergence reaches a residual of 1e-8 (independent numpy residual)."""
+    P = grids.poisson_problem(20, seed=3)
+    o = oracle_mod.Oracle(P["x"], P["y"], P["z"], 100.0, 1.0, omega=1.85, eps=1e-8, criterion=1,
+                          max_sweeps=100000, check_every=1)
+    ay = o.acoef(1)                        # y: Neumann at both ends in the reference as well
+    assert np.array_equal(ay, P["acoef"][1])
+    ax = o.acoef(0)                        # x: the outlet row differs (Dirichlet there)
+    assert np.array_equal(ax[:-1], P["acoef"][0][:-1])
+    o.no_body()
+    o.set_acoef(*P["acoef"])
+    o.set_field("b", P["b"])
+    st = o.redblack_sor()
+    assert st["final_err"] < 1e-8
+    import importlib
+    res = importlib.import_module("test_gpu_poisson").residual
+    assert res(P, o.get_field("pc")) < 1e-8
