@@ -84,6 +84,47 @@ FAST = dict(precision=1, warm_start=1, criterion=1, inner_sweeps=256, omega_inne
             max_sweeps=400000)
 PLAIN = dict(precision=0, warm_start=0, criterion=1, check_every=8, max_sweeps=400000)
 SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
+# U-Net weights trained on the GPU by this library's own kernels (bench.py --train-net)
+WEIGHTS = ROOT / "ib3d-gpu_gb300" / "weights" / "unet_sphere256.f32"
+
+
+def load_net(pkg, path=WEIGHTS):
+    """The trained warm-start network, or None when no weights file exists."""
+    import numpy as np
+    if not pathlib.Path(path).exists():
+        return None
+    net = pkg.Net(seed=0)
+    w = np.fromfile(path, dtype="<f4")
+    if w.size != net.nparams:
+        raise SystemExit(f"{path}: {w.size} weights, the network has {net.nparams}")
+    net.set_params(w)
+    return net
+
+
+def train_net(pkg, cs, out: str, seconds: float) -> dict:
+    """Generates snapshots (4 perturbed runs at Re 200/250/300/350, 24 steps, 16 random
+    64^3 patches per step from step 3), trains with Adam for `seconds` (batch 8, lr 1e-3
+    then 2e-4 for the last 30 %) and writes the FP32 weights."""
+    import dataclasses
+    import numpy as np
+    learned = importlib.import_module("ib3d_gpu_gb300.learned")
+    net = pkg.Net(seed=0)
+    net.reserve(64, 4 * 24 * 16)
+    gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 16)
+    fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
+    before = fit()
+    t0, steps = time.perf_counter(), 0
+    while time.perf_counter() - t0 < seconds:
+        lr = 1e-3 if time.perf_counter() - t0 < 0.7 * seconds else 2e-4
+        learned.train(net, 100, batch=8, lr=lr, chunk=100, seed=steps)
+        steps += 100
+    after = fit()
+    pathlib.Path(out).parent.mkdir(parents=True, exist_ok=True)
+    net.get_params().astype("<f4").tofile(out)
+    ev = learned.evaluate(net, dataclasses.replace(cs), 275.0, 12)
+    return {"weights": str(out), "patches": gen["patches"], "generate_s": gen["seconds"], "adam_steps": steps,
+            "train_s": time.perf_counter() - t0, "training_set_loss": [before, after],
+            "eval_re275": {k: {"sweeps": v["sweeps"], "seconds": v["seconds"]} for k, v in ev.items()}}
 
 
 # ------------------------------------------------------------------ clocks
@@ -166,9 +207,12 @@ class Dist:
 
 # -------------------------------------------------------------- GPU arms
 
-def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bool = True, clocks=None):
+def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bool = True, clocks=None,
+            net=None):
     import torch
     s = pkg.setup_case(cs, **mode)
+    if net is not None:
+        s.attach_net(net)
     first = True
     for _ in range(warmup):
         s.step(first)
@@ -328,10 +372,14 @@ def main():
     ap.add_argument("--poisson", type=int, default=0,
                     help="instead of the step benchmark: the standalone all-Neumann Poisson cube of this edge "
                          "(omega 1.85, residual 1e-8), FP64 and FP32-sweep forms")
+    ap.add_argument("--train-net", default="",
+                    help="instead of the benchmark: generate snapshots, train the warm-start U-Net and write "
+                         "its weights to this file")
+    ap.add_argument("--train-seconds", type=float, default=300.0)
     ap.add_argument("--set", default="",
                     help="comma-separated key=value overrides of the FP32-sweep arm's solver parameters")
-    ap.add_argument("--arms", default="fast,plain,e2e,cpu",
-                    help="comma-separated subset of fast,plain,e2e,cpu (profiling runs use 'fast')")
+    ap.add_argument("--arms", default="fast,learned,plain,e2e,cpu",
+                    help="comma-separated subset of fast,learned,plain,e2e,cpu (profiling runs use 'fast')")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
     dist = Dist()
@@ -339,6 +387,12 @@ def main():
     for kv in filter(None, args.set.split(",")):
         k, v = kv.split("=")
         FAST[k.strip()] = float(v) if "." in v or "e" in v else int(v)
+    if args.train_net:
+        if dist.rank == 0:
+            print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds)),
+                  flush=True)
+        dist.close()
+        return
     if args.poisson:
         if dist.rank == 0:
             print(json.dumps(run_poisson(pkg, args.poisson)), flush=True)
@@ -399,6 +453,20 @@ def main():
     phase_total = sum(tm[f"{p}_ms"] for p in pkg.Timers.PHASES)
 
     arms = set(args.arms.split(","))
+    learned_line = None
+    net = load_net(pkg) if "learned" in arms else None
+    if net is not None:
+        lmode = dict(FAST, warm_start=pkg.WARM_LEARNED)
+        lrn = run_arm(pkg, cs, lmode, warmup, args.steps, dist, timers=True, net=net)
+        lt = dist.max(lrn["seconds"])
+        ltm = lrn["timers"]
+        lsweeps = sum(st["sweeps"] for st in lrn["stats"]) / args.steps
+        learned_line = {"value": dist.world * args.steps / lt, "unit": "steps/s",
+                        "ms_per_step": 1e3 * lt / args.steps, "sweeps_per_step": lsweeps,
+                        "sweeps_saved_vs_previous_correction": 1.0 - lsweeps / (sweeps / args.steps),
+                        "net_ms_per_step": ltm["net_ms"] / args.steps,
+                        "drag_lift": lrn["coef"], "weights": str(WEIGHTS.relative_to(ROOT))}
+        net.close()
     plain_steps = max(1, min(args.plain_steps, args.steps))
     if "plain" in arms:
         plain = run_arm(pkg, cs, PLAIN, warmup, plain_steps, dist, timers=True)
@@ -436,6 +504,9 @@ def main():
                        "ms_per_sweep": t_sweep64 * 1e3 if t_sweep64 else None,
                        "sweep_bound": "FP64 ALU (GB300 FP64 ~0.5 TFMA/s measured)"},
         "speedup_vs_plain_fp64": value / plain_value if plain_value else None,
+        "learned_fp32": learned_line,
+        "learned_speedup_vs_plain_fp64": (learned_line["value"] / plain_value
+                                          if learned_line and plain_value else None),
         "sweeps_per_step": sweeps / args.steps,
         "sweeps_per_s": tm["sweeps32"] / (tm["sor32_ms"] * 1e-3) if tm["sor32_ms"] else None,
         "cells_per_s": value * ncell,

@@ -27,14 +27,18 @@ LIB_PATH = HERE / "libib3d.so"
 HEADER = HERE.parent / "include" / "ib3d.h"
 
 OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMORY, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
+ERR_IO = -9
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
 PREC_FP64, PREC_FP32DC = 0, 1
 WARM_ZERO, WARM_PREV, WARM_LEARNED = 0, 1, 2
 INNER_FIXED, INNER_ADAPTIVE = 0, 1
+MESH_GMSH, MESH_GAMBIT = 0, 1
+OUTLET_ZERO_GRADIENT, OUTLET_CONVECTIVE = 0, 1
+MOMENTUM_EULER, MOMENTUM_AB2 = 0, 1
 FIELDS = {"u": 0, "v": 1, "w": 2, "ut": 3, "vt": 4, "wt": 5, "p": 6, "pc": 7, "b": 8}
 _ERRNAMES = {ERR_ARG: "IB3D_ERR_ARG", ERR_CUDA: "IB3D_ERR_CUDA", ERR_MESH: "IB3D_ERR_MESH",
              ERR_PROBE: "IB3D_ERR_PROBE", ERR_NOCONV: "IB3D_ERR_NOCONV", ERR_NONFINITE: "IB3D_ERR_NONFINITE",
-             ERR_MEMORY: "IB3D_ERR_MEMORY", ERR_TOO_LARGE: "IB3D_ERR_TOO_LARGE"}
+             ERR_MEMORY: "IB3D_ERR_MEMORY", ERR_TOO_LARGE: "IB3D_ERR_TOO_LARGE", ERR_IO: "IB3D_ERR_IO"}
 
 
 class IB3DError(RuntimeError):
@@ -47,7 +51,8 @@ class Params(C.Structure):
     _fields_ = [("re", C.c_double), ("deltat", C.c_double), ("omega", C.c_double), ("eps", C.c_double),
                 ("max_sweeps", C.c_int64), ("criterion", C.c_int32), ("precision", C.c_int32),
                 ("warm_start", C.c_int32), ("check_every", C.c_int32), ("inner_sweeps", C.c_int32),
-                ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double), ("inner_schedule", C.c_int32)]
+                ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double), ("inner_schedule", C.c_int32),
+                ("outlet", C.c_int32), ("momentum", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -102,6 +107,15 @@ def lib() -> C.CDLL:
                                     C.c_double, C.c_double, C.c_int64]),
         "ib3d_search": (C.c_int, [_VP, _I64, _I64]),
         "ib3d_move_body": (C.c_int, [_VP] + [C.c_double] * 6),
+        "ib3d_move_body_free": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _D]),
+        "ib3d_read_surface_mesh": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, _I64, _D, _D, _D, _I64, _I64, _I64,
+                                             _I64]),
+        "ib3d_set_mesh_file": (C.c_int, [_VP, C.c_char_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
+                                         C.c_double, C.c_int64]),
+        "ib3d_write_restart": (C.c_int, [_VP, C.c_char_p, C.c_double, C.c_int64, C.c_int64]),
+        "ib3d_read_restart": (C.c_int, [_VP, C.c_char_p, _D, _I64, _I64]),
+        "ib3d_write_result_text": (C.c_int, [_VP, C.c_char_p, C.c_double, C.c_int64, C.c_int64]),
+        "ib3d_read_result_text": (C.c_int, [_VP, C.c_char_p, _D, _I64, _I64]),
         "ib3d_set_poisson_coefficients": (C.c_int, [_VP, _D, _D, _D]),
         "ib3d_get_search": (C.c_int, [_VP, _I64, _I64, _I64, _D]),
         "ib3d_initial_conditions": (C.c_int, [_VP]),
@@ -110,6 +124,8 @@ def lib() -> C.CDLL:
         "ib3d_get_field": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_set_field": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_ns_momentum": (C.c_int, [_VP]),
+        "ib3d_ns_momentum_ab": (C.c_int, [_VP]),
+        "ib3d_calculate_uc": (C.c_int, [_VP, _D]),
         "ib3d_velocity_bc": (C.c_int, [_VP]),
         "ib3d_solid_cell_bc": (C.c_int, [_VP]),
         "ib3d_velocity_forcing": (C.c_int, [_VP]),
@@ -237,6 +253,29 @@ class Solver:
         self._check(self.L.ib3d_set_poisson_coefficients(self._h, *(_dp(v) for v in a)),
                     "ib3d_set_poisson_coefficients")
 
+    def write_restart(self, path, totime: float = 0.0, ita: int = 0, ita1: int = 0, text: bool = False):
+        """Binary restart (or, text=True, the reference's formatted `result` file)."""
+        fn = self.L.ib3d_write_result_text if text else self.L.ib3d_write_restart
+        self._check(fn(self._h, str(path).encode(), float(totime), int(ita), int(ita1)), "write restart")
+
+    def read_restart(self, path, text: bool = False) -> tuple:
+        """Loads u, v, w, p (and ut = u ...); returns (totime, ita, ita1)."""
+        t = np.zeros(1)
+        it = np.zeros(2, dtype=np.int64)
+        fn = self.L.ib3d_read_result_text if text else self.L.ib3d_read_restart
+        self._check(fn(self._h, str(path).encode(), _dp(t), _ip(it[0:1]), _ip(it[1:2])), "read restart")
+        return float(t[0]), int(it[0]), int(it[1])
+
+    def move_body_free(self, fx: float, fy: float, fz: float) -> np.ndarray:
+        """Force-driven motion (shiftSurfaceNodesMovingbody); returns the new body velocity."""
+        v = np.zeros(3)
+        self._check(self.L.ib3d_move_body_free(self._h, fx, fy, fz, _dp(v)), "ib3d_move_body_free")
+        return v
+
+    def set_mesh_file(self, path, fmt: int = 0, sur_geo_points: int = 0, shift=(0.0, 0.0, 0.0), inor: int = 1):
+        self._check(self.L.ib3d_set_mesh_file(self._h, str(path).encode(), fmt, sur_geo_points, float(shift[0]),
+                                              float(shift[1]), float(shift[2]), inor), "ib3d_set_mesh_file")
+
     def move_body(self, dx: float, dy: float, dz: float, us: float = 0.0, vs: float = 0.0, ws: float = 0.0):
         """Prescribed motion: shift the body, set its velocity; search again before stepping."""
         self._check(self.L.ib3d_move_body(self._h, dx, dy, dz, us, vs, ws), "ib3d_move_body")
@@ -324,6 +363,14 @@ class Solver:
         d = st.as_dict()
         d["rc"] = rc
         return d
+
+    def ns_momentum_ab(self):
+        self._check(self.L.ib3d_ns_momentum_ab(self._h), "ib3d_ns_momentum_ab")
+
+    def calculate_uc(self) -> float:
+        uc = np.zeros(1)
+        self._check(self.L.ib3d_calculate_uc(self._h, _dp(uc)), "ib3d_calculate_uc")
+        return float(uc[0])
 
     def redblack_sor(self, allow_noconv: bool = False) -> dict:
         """REDBLACKSOR alone on the b already set (set_field("b", ...))."""
@@ -415,6 +462,25 @@ class Net:
         loss = np.zeros(1)
         self._check(self.L.ib3d_net_train(self._h, steps, batch, lr, seed, loss.ctypes.data_as(_D)), "ib3d_net_train")
         return float(loss[0])
+
+
+def read_surface_mesh(path, fmt: int = 0, sur_geo_points: int = 0):
+    """Nodes (N,3) and 1-based triangles (M,3) of a Gmsh 2 or Gambit surface mesh file."""
+    L = lib()
+    nn = np.zeros(1, np.int64)
+    ne = np.zeros(1, np.int64)
+    null = C.POINTER(C.c_double)()
+    rc = L.ib3d_read_surface_mesh(str(path).encode(), fmt, sur_geo_points, _ip(nn), null, null, null, _ip(ne),
+                                  C.POINTER(C.c_int64)(), C.POINTER(C.c_int64)(), C.POINTER(C.c_int64)())
+    if rc != OK:
+        raise IB3DError(rc, "ib3d_read_surface_mesh")
+    xyz = [np.zeros(int(nn[0])) for _ in range(3)]
+    e = [np.zeros(int(ne[0]), np.int64) for _ in range(3)]
+    rc = L.ib3d_read_surface_mesh(str(path).encode(), fmt, sur_geo_points, _ip(nn), *(_dp(a) for a in xyz), _ip(ne),
+                                  *(_ip(a) for a in e))
+    if rc != OK:
+        raise IB3DError(rc, "ib3d_read_surface_mesh")
+    return np.stack(xyz, axis=1), np.stack(e, axis=1)
 
 
 def setup_case(cs, params: Params | None = None, **kw) -> Solver:

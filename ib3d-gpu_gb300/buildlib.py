@@ -16,9 +16,10 @@ import subprocess
 HERE = pathlib.Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIB = HERE / "libib3d.so"
-SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu", "noalloc.cu", "k_momentum_fast.cu", "k_unet.cu", "unet.cu"]
+SOURCES = ["ib3d_api.cu", "k_pressure.cu", "k_momentum.cu", "k_ib.cu", "k_sor32.cu", "noalloc.cu", "k_momentum_fast.cu", "k_fast.cu", "k_unet.cu",
+           "unet.cu", "restart.cu", "mesh_io.cu"]
 # translation units whose multiply-adds may contract (results differ from the reference by rounding)
-FMAD_TRUE = {"k_momentum_fast.cu"}
+FMAD_TRUE = {"k_momentum_fast.cu", "k_fast.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -185,6 +185,7 @@ void fast_tables(const std::vector<double>& d, int n, int axis, const std::vecto
     const double hs = 0.5 * ((dm + dp) + (dm + dl));
     put(23, m, 2.0 / (hs * (0.5 * (dm + dp))));
     put(24, m, 2.0 / (hs * (0.5 * (dm + dl))));
+    put(25, m, 1.0 / dm);
   }
 }
 
@@ -227,6 +228,10 @@ int alloc_fields(ib3d_ctx* c) {
   if (cudaMallocHost(&c->h_ctl, sizeof(SolveCtl)) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->d_flag, sizeof(int)) != cudaSuccess) return IB3D_ERR_MEMORY;
   if (cudaMalloc(&c->d_coef, 8 * sizeof(double)) != cudaSuccess) return IB3D_ERR_MEMORY;
+  {
+    const double uc0 = 1.0;   // uc = 1 (subReadInput.f90:28); d_coef[6] holds the outlet speed
+    if (cudaMemcpy(c->d_coef + 6, &uc0, sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return IB3D_ERR_CUDA;
+  }
   c->scan_cap = 64;
   if (cudaMalloc(&c->d_scan, c->scan_cap * sizeof(long long)) != cudaSuccess) return IB3D_ERR_MEMORY;
   cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st);
@@ -239,7 +244,9 @@ bool valid_params(const ib3d_params* p) {
          (p->precision == 0 || p->precision == 1) && (p->warm_start >= 0 && p->warm_start <= 2) &&
          p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
-         (p->inner_schedule == IB3D_INNER_FIXED || p->inner_schedule == IB3D_INNER_ADAPTIVE);
+         (p->inner_schedule == IB3D_INNER_FIXED || p->inner_schedule == IB3D_INNER_ADAPTIVE) &&
+         (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&
+         (p->momentum == IB3D_MOMENTUM_EULER || p->momentum == IB3D_MOMENTUM_AB2);
 }
 
 int fail(ib3d_ctx* c, int code, const char* msg) {
@@ -306,10 +313,30 @@ void ib3d_default_params(ib3d_params* p) {
 
 const char* ib3d_last_error(const ib3d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
+// resi_u/v/w of nsMomentumAB, allocated (zeroed, subInitialConditions.f90:24) the
+// first time the Adams-Bashforth scheme is selected
+static int ensure_resi(ib3d_ctx* c, bool need) {
+  if (!need || c->resi[0]) return IB3D_OK;
+  for (int q = 0; q < 3; ++q) {
+    if (cudaMalloc(&c->resi[q], (size_t)c->d.n3 * sizeof(double)) != cudaSuccess)
+      return fail(c, IB3D_ERR_MEMORY, "nsMomentumAB residual arrays");
+    if (cudaMemsetAsync(c->resi[q], 0, (size_t)c->d.n3 * sizeof(double), c->st) != cudaSuccess)
+      return fail(c, IB3D_ERR_CUDA, "nsMomentumAB residual arrays");
+  }
+  return IB3D_OK;
+}
+
+static int zero_resi(ib3d_ctx* c) {
+  for (int q = 0; q < 3; ++q)
+    if (c->resi[q]) IB3D_CUDA(c, cudaMemsetAsync(c->resi[q], 0, (size_t)c->d.n3 * sizeof(double), c->st));
+  return IB3D_OK;
+}
+
 int ib3d_set_params(ib3d_ctx* ctx, const ib3d_params* prm) {
   if (!ctx) return IB3D_ERR_ARG;
   if (!valid_params(prm)) return fail(ctx, IB3D_ERR_ARG, "ib3d_set_params: invalid parameters");
   ctx->prm = *prm;
+  if (int rc = ensure_resi(ctx, prm->momentum == IB3D_MOMENTUM_AB2)) return rc;
   // the velocity-correction factors depend on deltat: rebuild them
   const double dt = prm->deltat;
   std::vector<double> cx((size_t)ctx->d.nx + 3, 0.0), cy((size_t)ctx->d.ny + 3, 0.0), cz((size_t)ctx->d.nz + 3, 0.0);
@@ -329,7 +356,7 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
   *out = nullptr;
   if (!valid_params(prm) || nx < 4 || ny < 4 || nz < 4 || !x1n || !y1n || !z1n) return IB3D_ERR_ARG;
   if ((nx + 2) * (ny + 2) * (nz + 2) >= (1ll << 31)) return IB3D_ERR_ARG;
-  if (nz > 65535) return IB3D_ERR_ARG;   // one grid z-index per plane in the FP32 sweep launch
+  if (nz > 65535) return IB3D_ERR_ARG;   // bounds the FP32 sweep launch's grid z-dimension
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return IB3D_ERR_CUDA;
   ib3d_ctx* c = new ib3d_ctx();
@@ -434,6 +461,7 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
       rc = IB3D_ERR_CUDA;
   }
   if (!rc) rc = alloc_fields(c);
+  if (!rc) rc = ensure_resi(c, prm->momentum == IB3D_MOMENTUM_AB2);
   if (!rc) rc = ib3d_set_params(c, prm);
   if (!rc && cudaStreamSynchronize(c->st) != cudaSuccess) rc = IB3D_ERR_CUDA;
   if (rc) {
@@ -453,7 +481,7 @@ void ib3d_destroy(ib3d_ctx* c) {
   void* ptrs[] = {c->d_tables, c->d_tables32, c->d_fast, c->d_axp, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
-                  c->hist[0], c->hist[1], c->r_hist};
+                  c->hist[0], c->hist[1], c->r_hist, c->resi[0], c->resi[1], c->resi[2]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -593,6 +621,7 @@ int ib3d_get_search(ib3d_ctx* c, int64_t* cell, int64_t* ib_list, int64_t* nelp,
 
 int ib3d_initial_conditions(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
+  if (int rc = zero_resi(c)) return rc;   // resi_u = 0 (subInitialConditions.f90:24)
   launch_initial(c);
   IB3D_CUDA(c, cudaGetLastError());
   return IB3D_OK;
@@ -605,6 +634,7 @@ static double* field_ptr(ib3d_ctx* c, int which) {
 
 int ib3d_upload_fields(ib3d_ctx* c, const double* u, const double* v, const double* w, const double* p) {
   if (!c) return IB3D_ERR_ARG;
+  if (int rc = zero_resi(c)) return rc;   // lastConditions: resi_u = 0 (subLastConditions.f90:16)
   const size_t bytes = (size_t)c->d.n3 * sizeof(double);
   const double* src[3] = {u, v, w};
   double* dst[3] = {c->u, c->v, c->w};
@@ -686,9 +716,29 @@ int ib3d_synchronize(ib3d_ctx* c) {
 
 int ib3d_ns_momentum(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
-  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c);
-  else launch_momentum(c);
+  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c, false);
+  else launch_momentum(c, false);
   IB3D_CUDA(c, cudaGetLastError());
+  return IB3D_OK;
+}
+
+int ib3d_ns_momentum_ab(ib3d_ctx* c) {
+  if (!c) return IB3D_ERR_ARG;
+  if (int rc = ensure_resi(c, true)) return rc;
+  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c, true);
+  else launch_momentum(c, true);
+  IB3D_CUDA(c, cudaGetLastError());
+  return IB3D_OK;
+}
+
+int ib3d_calculate_uc(ib3d_ctx* c, double* uc) {
+  if (!c) return IB3D_ERR_ARG;
+  launch_calculate_uc(c);
+  IB3D_CUDA(c, cudaGetLastError());
+  if (uc) {
+    IB3D_CUDA(c, cudaMemcpyAsync(uc, c->d_coef + 6, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  }
   return IB3D_OK;
 }
 
@@ -747,7 +797,8 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
   IB3D_CUDA(c, cudaMemsetAsync(red, 0, 2 * sizeof(unsigned long long), c->st));
   // divergence writes its max into ctl->aux; copy it aside before the SOR resets ctl
   IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
-  launch_divergence(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  if (c->prm.precision == IB3D_PREC_FP32DC) launch_divergence_fast(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  else launch_divergence(c, c->prm.warm_start == IB3D_WARM_ZERO);
   if (c->r_hist) {
     PhaseScope ps(c, PH_NET);
     net_hist_residual(c);   // the current guess's residual: a network input and a capture input
@@ -825,7 +876,11 @@ int ib3d_step(ib3d_ctx* c, int first, ib3d_solve_stats* stats, double coef[4]) {
   if (!c->searched) return fail(c, IB3D_ERR_ARG, "ib3d_step: call ib3d_search first");
   int rc;
   c->t_steps += 1;
-  if ((rc = ib3d_ns_momentum(c))) return rc;        // main.f90:46
+  if (c->prm.momentum == IB3D_MOMENTUM_AB2 && !first) {
+    if ((rc = ib3d_ns_momentum_ab(c))) return rc;   // main.f90:45 (nsMomentumAB)
+  } else if ((rc = ib3d_ns_momentum(c))) {         // main.f90:46 (30 on the first step)
+    return rc;
+  }
   if ((rc = ib3d_velocity_bc(c))) return rc;        // :47
   if ((rc = ib3d_solid_cell_bc(c))) return rc;      // :48
   if ((rc = ib3d_velocity_forcing(c))) return rc;   // :49
@@ -833,6 +888,8 @@ int ib3d_step(ib3d_ctx* c, int first, ib3d_solve_stats* stats, double coef[4]) {
   const int prc = ib3d_poisson_solver(c, stats);    // :51
   if (prc && prc != IB3D_ERR_NOCONV) return prc;
   if ((rc = ib3d_pressure_forcing(c))) return rc;   // :52
+  if (c->prm.outlet == IB3D_OUTLET_CONVECTIVE)      // the calculateUc hook, :53-54
+    if ((rc = ib3d_calculate_uc(c, nullptr))) return rc;
   if ((rc = ib3d_stress(c, first, coef))) return rc;  // :64 (stressCal1 at :39)
   return prc;
 }

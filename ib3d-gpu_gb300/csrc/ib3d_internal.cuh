@@ -22,7 +22,7 @@
 namespace ib3d {
 
 constexpr int kBlock = 256;
-constexpr int kFastTables = 25;   // 1-D tables per axis of the fast momentum kernel
+constexpr int kFastTables = 26;   // 1-D tables per axis of the fast kernels (k_momentum_fast.cu, k_fast.cu)
 
 // Index helpers: 1-based Fortran (i,j,k) into the padded column-major array.
 struct Dims {
@@ -118,6 +118,9 @@ struct ib3d_ctx {
   ib3d::Grid1D g{};
   double *u = nullptr, *v = nullptr, *w = nullptr, *ut = nullptr, *vt = nullptr, *wt = nullptr;
   double *p = nullptr, *pc = nullptr, *b = nullptr, *bdt = nullptr;
+  // resi_u/v/w: the previous step's convection-diffusion residual (nsMomentumAB), kept
+  // only when ib3d_params.momentum is IB3D_MOMENTUM_AB2
+  double* resi[3] = {nullptr, nullptr, nullptr};
   float *e32 = nullptr, *r32 = nullptr;
   // colour-packed FP32 arrays of the inner solve ([0] red, [1] black); see k_sor32.cu
   float* ep[2] = {nullptr, nullptr};
@@ -186,17 +189,21 @@ struct ib3d_ctx {
 namespace ib3d {
 // k_pressure.cu
 void launch_divergence(ib3d_ctx* c, bool zero_pc);
+// k_fast.cu: FMA-contracted FP64 kernels of the IB3D_PREC_FP32DC path
+void launch_divergence_fast(ib3d_ctx* c, bool zero_pc);
+void launch_residual_fast(ib3d_ctx* c, long long sweep);
 void launch_bdt(ib3d_ctx* c, bool zero_pc);
 int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st);
 int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st);
 void launch_correct(ib3d_ctx* c);
 void launch_velocity_bc(ib3d_ctx* c);
+void launch_calculate_uc(ib3d_ctx* c);
 void launch_solid_bc(ib3d_ctx* c);
 void launch_dss_copy(ib3d_ctx* c);
 void launch_initial(ib3d_ctx* c);
 // k_momentum.cu, k_momentum_fast.cu
-void launch_momentum(ib3d_ctx* c);
-void launch_momentum_fast(ib3d_ctx* c);
+void launch_momentum(ib3d_ctx* c, bool ab2);
+void launch_momentum_fast(ib3d_ctx* c, bool ab2);
 // k_sor32.cu
 int packed_row_length(int nx);
 void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1);
@@ -257,26 +264,65 @@ namespace ib3d {
 __device__ __forceinline__ double nan_max(double a, double b) {
   return (a != a) ? a : ((b > a || b != b) ? b : a);
 }
-__device__ __forceinline__ double warp_max(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_down_sync(0xffffffffu, v, o));
+// Block-wide max of a non-negative double (an fabs result, or a NaN from one), then
+// one atomicMax on its bit pattern. For non-negative IEEE doubles the unsigned order
+// of the bit patterns is the numeric order, and a NaN with the sign bit clear orders
+// above +inf, so the max is exact, a NaN still reaches the host check, and the
+// reduction runs on the integer units rather than the FP64 pipe (on this part the
+// FP64 compares of a floating-point reduction cost as much as a stencil's FMAs).
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
   return v;
 }
-// Block-wide max of a non-negative double, then one atomicMax on its bit pattern
-// (for non-negative IEEE doubles the integer order equals the numeric order).
 __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* slot) {
-  __shared__ double sm[32];
-  v = warp_max(v);
+  __shared__ unsigned long long sm[32];
+  const unsigned long long b = warp_max_bits((unsigned long long)__double_as_longlong(v));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sm[wid] = v;
+  if (lane == 0) sm[wid] = b;
   __syncthreads();
   if (wid == 0) {
     const int nw = (int)((blockDim.x * blockDim.y * blockDim.z + 31) >> 5);
-    double x = lane < nw ? sm[lane] : 0.0;
-    x = warp_max(x);
-    if (lane == 0 && !(x <= 0.0)) atomicMax(slot, (unsigned long long)__double_as_longlong(x));
+    unsigned long long x = lane < nw ? sm[lane] : 0ull;
+    x = warp_max_bits(x);
+    if (lane == 0 && x != 0ull) atomicMax(slot, x);
   }
 }
 __device__ __forceinline__ double bits_to_double(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// The finishing step shared by every kernel that ends a sweep or a check: the
+// last block to retire reads the accumulated maximum, applies the stopping test
+// (continue while err >= eps, subPcorVcor.f90:210) and the sweep cap, and resets
+// the accumulator. Returns nothing; the decision lands in ctl for the next kernel
+// and for the host.
+__device__ __forceinline__ void finish_block(SolveCtl* ctl, unsigned long long* acc, int mode, long long sweep,
+                                             double eps, long long max_sweeps) {
+  // mode 0: test acc against eps, then the cap; 1: only the cap; 2: no decision
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned ticket = atomicAdd(&ctl->tickets, 1u);
+    if (ticket == nb - 1) {
+      __threadfence();
+      const double err = bits_to_double(atomicExch(acc, 0ull));
+      ctl->tickets = 0;
+      if (mode == 0) {
+        ctl->last_res = err;
+        if (!(err >= eps)) {
+          ctl->done = 1; ctl->nsweeps = sweep; ctl->final_err = err;
+        } else if (sweep >= max_sweeps) {
+          ctl->done = 2; ctl->nsweeps = sweep; ctl->final_err = err;
+        }
+      } else if (mode == 1) {
+        if (sweep >= max_sweeps) { ctl->done = 2; ctl->nsweeps = sweep; ctl->final_err = ctl->last_res; }
+      }
+      __threadfence();
+    }
+  }
+}
 
 // The FP32 SOR update shared by every FP32 sweep kernel: e <- (1-omega) e +
 // omega num / diag, the quotient through the hardware reciprocal (two

@@ -42,7 +42,8 @@ __global__ void __launch_bounds__(128) k_momentum(Dims d, Grid1D g, const double
                                                   const double* __restrict__ P,
                                                   const unsigned char* __restrict__ C, double* __restrict__ UT,
                                                   double* __restrict__ VT, double* __restrict__ WT, double rev,
-                                                  double deltat) {
+                                                  double deltat, double* __restrict__ RU, double* __restrict__ RV,
+                                                  double* __restrict__ RW, int ab2) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) return;
   const int i = (int)(tid % (unsigned)d.nx) + 2;
@@ -106,7 +107,9 @@ __global__ void __launch_bounds__(128) k_momentum(Dims d, Grid1D g, const double
     const double d2z = (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-u12 / (0.5 * dz2zt)) + (u10 / (0.5 * dz2zb)));
     const double xtt2 = rev * (d2x + d2y + d2z);
     const double resid = -cx - cy - cz + xtt2;
-    UT[o] = u0 + deltat * (resid + dpdx);
+    if (ab2) UT[o] = u0 + deltat * (0.5 * (3.0 * resid - RU[o]) + dpdx);   // nsMomentumAB
+    else UT[o] = u0 + deltat * (resid + dpdx);
+    if (RU) RU[o] = resid;
   }
   // ---- v momentum (:901-1006)
   {
@@ -133,7 +136,9 @@ __global__ void __launch_bounds__(128) k_momentum(Dims d, Grid1D g, const double
     const double d2z = (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-v14 / (0.5 * dz2zt)) + (v12 / (0.5 * dz2zb)));
     const double ytt2 = rev * (d2x + d2y + d2z);
     const double resid = -cx - cy - cz + ytt2;
-    VT[o] = v0 + deltat * (resid + dpdy);
+    if (ab2) VT[o] = v0 + deltat * (0.5 * (3.0 * resid - RV[o]) + dpdy);   // nsMomentumAB
+    else VT[o] = v0 + deltat * (resid + dpdy);
+    if (RV) RV[o] = resid;
   }
   // ---- w momentum (:1010-1116)
   {
@@ -160,17 +165,20 @@ __global__ void __launch_bounds__(128) k_momentum(Dims d, Grid1D g, const double
     const double d2z = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
     const double ztt2 = rev * (d2x + d2y + d2z);
     const double resid = -cx - cy - cz + ztt2;
-    WT[o] = w0 + deltat * (resid + dpdz);
+    if (ab2) WT[o] = w0 + deltat * (0.5 * (3.0 * resid - RW[o]) + dpdz);   // nsMomentumAB
+    else WT[o] = w0 + deltat * (resid + dpdz);
+    if (RW) RW[o] = resid;
   }
 }
 
-void launch_momentum(ib3d_ctx* c) {
+void launch_momentum(ib3d_ctx* c, bool ab2) {
   PhaseScope ps(c, PH_MOMENTUM);
   c->launches += 1;
   const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;
   const unsigned nb = (unsigned)((n + 127) / 128);
   k_momentum<<<nb, 128, 0, c->st>>>(c->d, c->g, c->u, c->v, c->w, c->p, c->cell, c->ut, c->vt, c->wt,
-                                     1.0 / c->prm.re, c->prm.deltat);
+                                     1.0 / c->prm.re, c->prm.deltat, c->resi[0], c->resi[1], c->resi[2],
+                                     ab2 ? 1 : 0);
 }
 
 }  // namespace ib3d

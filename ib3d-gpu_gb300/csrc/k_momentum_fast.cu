@@ -18,6 +18,7 @@
 //   13..20  first-order half: same with r = 0.5(d[m]+d[m-1])/(0.5(d[m]+d[m+1])), dA = 0.5(d[m]+d[m+1])
 //   21 cna  2/((d[m]+d[m+1]) d[m+1])   22 cnb 2/((d[m]+d[m+1]) d[m])       node diffusion
 //   23 cha  2/(0.5(2d[m]+d[m+1]+d[m-1]) 0.5(d[m]+d[m+1]))  24 chb  .../0.5(d[m]+d[m-1])  half diffusion
+//   25 rd   1/d[m]                                reciprocal spacing (divergence, k_fast.cu)
 #include "ib3d_internal.cuh"
 
 namespace ib3d {
@@ -60,7 +61,8 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
                                                        const double* __restrict__ W, const double* __restrict__ P,
                                                        const unsigned char* __restrict__ C, double* __restrict__ UT,
                                                        double* __restrict__ VT, double* __restrict__ WT, double rev,
-                                                       double deltat) {
+                                                       double deltat, double* __restrict__ RU,
+                                                       double* __restrict__ RV, double* __restrict__ RW, int ab2) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) return;
   const int i = (int)(tid % (unsigned)d.nx) + 2;
@@ -95,7 +97,9 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
                       F(1, 24, j) * (U[o - sy] - u0) - F(1, 23, j) * (u0 - U[o + sy]) +
                       F(2, 24, k) * (U[o - sz] - u0) - F(2, 23, k) * (u0 - U[o + sz]);
     const double resid = fma(rev, d2, -cx - cy - cz);
-    UT[o] = fma(deltat, resid, u0) + g.corx[i] * (p0 - P[o + sx]);
+    const double rhs = ab2 ? 0.5 * (3.0 * resid - RU[o]) : resid;   // nsMomentumAB or nsMomentum
+    UT[o] = fma(deltat, rhs, u0) + g.corx[i] * (p0 - P[o + sx]);
+    if (RU) RU[o] = resid;
   }
   // ---- v: own axis y
   {
@@ -116,7 +120,9 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
                       F(1, 22, j) * (V[o - sy] - v0) - F(1, 21, j) * (v0 - V[o + sy]) +
                       F(2, 24, k) * (V[o - sz] - v0) - F(2, 23, k) * (v0 - V[o + sz]);
     const double resid = fma(rev, d2, -cx - cy - cz);
-    VT[o] = fma(deltat, resid, v0) + g.cory[j] * (p0 - P[o + sy]);
+    const double rhs = ab2 ? 0.5 * (3.0 * resid - RV[o]) : resid;   // nsMomentumAB or nsMomentum
+    VT[o] = fma(deltat, rhs, v0) + g.cory[j] * (p0 - P[o + sy]);
+    if (RV) RV[o] = resid;
   }
   // ---- w: own axis z
   {
@@ -137,18 +143,21 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
                       F(1, 24, j) * (W[o - sy] - w0) - F(1, 23, j) * (w0 - W[o + sy]) +
                       F(2, 22, k) * (W[o - sz] - w0) - F(2, 21, k) * (w0 - W[o + sz]);
     const double resid = fma(rev, d2, -cx - cy - cz);
-    WT[o] = fma(deltat, resid, w0) + g.corz[k] * (p0 - P[o + sz]);
+    const double rhs = ab2 ? 0.5 * (3.0 * resid - RW[o]) : resid;   // nsMomentumAB or nsMomentum
+    WT[o] = fma(deltat, rhs, w0) + g.corz[k] * (p0 - P[o + sz]);
+    if (RW) RW[o] = resid;
   }
   (void)m3;
 }
 
-void launch_momentum_fast(ib3d_ctx* c) {
+void launch_momentum_fast(ib3d_ctx* c, bool ab2) {
   PhaseScope ps(c, PH_MOMENTUM);
   c->launches += 1;
   const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;
   k_momentum_fast<<<(unsigned)((n + 127) / 128), 128, 0, c->st>>>(c->d, c->g, c->d_fast, c->fast_stride, c->u, c->v,
                                                                    c->w, c->p, c->cell, c->ut, c->vt, c->wt,
-                                                                   1.0 / c->prm.re, c->prm.deltat);
+                                                                   1.0 / c->prm.re, c->prm.deltat, c->resi[0],
+                                                                   c->resi[1], c->resi[2], ab2 ? 1 : 0);
 }
 
 }  // namespace ib3d

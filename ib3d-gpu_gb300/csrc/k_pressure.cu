@@ -31,38 +31,6 @@ __device__ __forceinline__ bool interior(const Dims& d, int i, int j, int k) {
 }
 inline unsigned nblocks(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
-// The finishing step shared by every kernel that ends a sweep or a check: the
-// last block to retire reads the accumulated maximum, applies the stopping test
-// (continue while err >= eps, subPcorVcor.f90:210) and the sweep cap, and resets
-// the accumulator. Returns nothing; the decision lands in ctl for the next kernel
-// and for the host.
-__device__ __forceinline__ void finish_block(SolveCtl* ctl, unsigned long long* acc, int mode, long long sweep,
-                                             double eps, long long max_sweeps) {
-  // mode 0: test acc against eps, then the cap; 1: only the cap; 2: no decision
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned ticket = atomicAdd(&ctl->tickets, 1u);
-    if (ticket == nb - 1) {
-      __threadfence();
-      const double err = bits_to_double(atomicExch(acc, 0ull));
-      ctl->tickets = 0;
-      if (mode == 0) {
-        ctl->last_res = err;
-        if (!(err >= eps)) {
-          ctl->done = 1; ctl->nsweeps = sweep; ctl->final_err = err;
-        } else if (sweep >= max_sweeps) {
-          ctl->done = 2; ctl->nsweeps = sweep; ctl->final_err = err;
-        }
-      } else if (mode == 1) {
-        if (sweep >= max_sweeps) { ctl->done = 2; ctl->nsweeps = sweep; ctl->final_err = ctl->last_res; }
-      }
-      __threadfence();
-    }
-  }
-}
-
 }  // namespace
 
 // computeDiv (subPcorVcor.f90:82-101) fused with the zeroing of b and pc
@@ -237,7 +205,9 @@ __global__ void __launch_bounds__(kBlock) k_correct(Dims d, Grid1D g, const doub
 
 // velocityBC, active branch (subBoundaryConditions.f90:350-406): x faces (inlet
 // u = 1, v/w reflected; outlet zero gradient), then y and z faces (slip).
-__global__ void k_bc_x(Dims d, double* ut, double* vt, double* wt) {
+__global__ void k_bc_x(Dims d, Grid1D g, double* ut, double* vt, double* wt, const double* __restrict__ u,
+                       const double* __restrict__ v, const double* __restrict__ w, const double* __restrict__ ucp,
+                       double deltat, int convective) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (unsigned)d.ny * (unsigned)d.nz) return;
   const int j = (int)(tid % (unsigned)d.ny) + 2, k = (int)(tid / (unsigned)d.ny) + 2;
@@ -245,9 +215,55 @@ __global__ void k_bc_x(Dims d, double* ut, double* vt, double* wt) {
   ut[d.at(1, j, k)] = 1.0;
   vt[d.at(1, j, k)] = -vt[d.at(2, j, k)];
   wt[d.at(1, j, k)] = -wt[d.at(2, j, k)];
-  ut[d.at(nx + 1, j, k)] = ut[d.at(nx, j, k)];
-  vt[d.at(nx + 2, j, k)] = vt[d.at(nx + 1, j, k)];
-  wt[d.at(nx + 2, j, k)] = wt[d.at(nx + 1, j, k)];
+  if (convective) {   // Orlanski (the commented :153-155), uc from calculateUc
+    const double uc = *ucp;
+    const long long a = d.at(nx + 1, j, k), b2 = d.at(nx + 2, j, k), a0 = d.at(nx, j, k);
+    ut[a] = u[a] - (deltat / g.dx[nx + 1]) * uc * (u[a] - u[a0]);
+    vt[b2] = -vt[a] + v[b2] + v[a] - (2.0 * deltat / g.dx[nx + 2]) * uc * (v[b2] - v[a]);
+    wt[b2] = -wt[a] + w[b2] + w[a] - (2.0 * deltat / g.dx[nx + 2]) * uc * (w[b2] - w[a]);
+  } else {            // zero gradient (:149-151)
+    ut[d.at(nx + 1, j, k)] = ut[d.at(nx, j, k)];
+    vt[d.at(nx + 2, j, k)] = vt[d.at(nx + 1, j, k)];
+    wt[d.at(nx + 2, j, k)] = wt[d.at(nx + 1, j, k)];
+  }
+}
+
+// calculateUc (subCalculateuc.f90:2-38): uc = max(mean of ut(nx-4,j,k) over the
+// plane's fluid cells, 0). One warp; the sum runs in the serial order k outer, j
+// inner (lane 0 adds the warp's 32 loaded values one by one), so it matches a
+// serial build of the reference bit for bit.
+__global__ void k_calculate_uc(Dims d, const double* __restrict__ ut, const unsigned char* __restrict__ cell,
+                               double* ucp) {
+  const int lane = threadIdx.x;
+  const int i = d.nx - 4;
+  double sum = 0.0;
+  long long count = 0;
+  for (int k = 2; k <= d.nz + 1; ++k)
+    for (int j0 = 2; j0 <= d.ny + 1; j0 += 32) {
+      const int j = j0 + lane;
+      double x = 0.0;
+      int fl = 0;
+      if (j <= d.ny + 1) {
+        const long long o = d.at(i, j, k);
+        fl = cell[o] == 0;
+        x = fl ? ut[o] : 0.0;
+      }
+      for (int l = 0; l < 32; ++l) {
+        const double xl = __shfl_sync(0xffffffffu, x, l);
+        const int fll = __shfl_sync(0xffffffffu, fl, l);
+        if (fll) { sum = sum + xl; ++count; }
+      }
+    }
+  if (lane == 0) {
+    const double uc1 = sum / (double)count;
+    *ucp = uc1 > 0.0 ? uc1 : 0.0;
+  }
+}
+
+void launch_calculate_uc(ib3d_ctx* c) {
+  PhaseScope ps(c, PH_BC);
+  c->launches += 1;
+  k_calculate_uc<<<1, 32, 0, c->st>>>(c->d, c->ut, c->cell, c->d_coef + 6);
 }
 __global__ void k_bc_y(Dims d, double* ut, double* vt, double* wt) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,7 +372,9 @@ void launch_velocity_bc(ib3d_ctx* c) {
   PhaseScope ps(c, PH_BC);
   c->launches += 3;
   const Dims& d = c->d;
-  k_bc_x<<<nblocks((long long)d.ny * d.nz), kBlock, 0, c->st>>>(d, c->ut, c->vt, c->wt);
+  k_bc_x<<<nblocks((long long)d.ny * d.nz), kBlock, 0, c->st>>>(d, c->g, c->ut, c->vt, c->wt, c->u, c->v, c->w,
+                                                                 c->d_coef + 6, c->prm.deltat,
+                                                                 c->prm.outlet == IB3D_OUTLET_CONVECTIVE ? 1 : 0);
   k_bc_y<<<nblocks((long long)d.nx * d.nz), kBlock, 0, c->st>>>(d, c->ut, c->vt, c->wt);
   k_bc_z<<<nblocks((long long)d.nx * d.ny), kBlock, 0, c->st>>>(d, c->ut, c->vt, c->wt);
 }
@@ -465,10 +483,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   for (;;) {
     {
       PhaseScope ps(c, PH_RESIDUAL);
-      c->launches += 1;
-      k_residual64<<<nblocks(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, packed ? nullptr : c->r32,
-                                                          packed ? c->rp[0] : nullptr, packed ? c->rp[1] : nullptr,
-                                                          c->packed_lp, c->ctl, sweeps, 0, P.eps, P.max_sweeps);
+      launch_residual_fast(c, sweeps);
     }
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);

@@ -58,7 +58,11 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
 
 // One colour pass. Block (32, 8): a warp covers 32 float4 groups of one row (j, k),
 // so the row's colour phase is uniform across the warp; grid (ceil(nq/32),
-// ceil(ny/8), nz) maps the rest without integer division.
+// ceil(ny/8), ceil(nz/kPlanes)) maps the rest without integer division. A thread
+// updates its four cells in kPlanes consecutive planes, carrying the other colour's
+// centre and upper plane over to the next plane instead of loading them again.
+constexpr int kPlanes = 2;
+
 template <int COLOR>
 __global__ void __launch_bounds__(256) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
                                                 float* __restrict__ e_own, const float* __restrict__ e_oth,
@@ -66,36 +70,44 @@ __global__ void __launch_bounds__(256) k_sor32p(Dims d, Grid1D g, const float* _
   const int nq = ((d.nx >> 1) + 3) >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y + 2;
-  const int k = blockIdx.z + 2;
+  const int k0 = blockIdx.z * kPlanes + 2;
   if (q >= nq || j > d.ny + 1) return;
   const long long plane = (long long)(d.ny + 2) * Lp;
-  const long long s0 = (long long)(k - 1) * plane + (long long)(j - 1) * Lp + 4 * q + 4;
-  // does this row start (i = 2) with the colour being updated?
-  const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
-  const float4 rr = *reinterpret_cast<const float4*>(r_own + s0);
-  const float4 eo = *reinterpret_cast<const float4*>(e_own + s0);
-  const float4 ox = *reinterpret_cast<const float4*>(e_oth + s0);
-  const float4 os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
-  const float4 on = *reinterpret_cast<const float4*>(e_oth + s0 + Lp);
-  const float4 ob = *reinterpret_cast<const float4*>(e_oth + s0 - plane);
-  const float4 ot = *reinterpret_cast<const float4*>(e_oth + s0 + plane);
-  const float left = e_oth[s0 - 1], right = e_oth[s0 + 4];
-  const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
-  const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
-  const float sv[4] = {os.x, os.y, os.z, os.w};
-  const float nv[4] = {on.x, on.y, on.z, on.w};
-  const float bv[4] = {ob.x, ob.y, ob.z, ob.w};
-  const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
-  float ev[4] = {eo.x, eo.y, eo.z, eo.w};
+  const long long sj = (long long)(j - 1) * Lp + 4 * q + 4;
   const float ay0 = g.acy32[0][j - 1], ay1 = g.acy32[1][j - 1], ay2 = g.acy32[2][j - 1];
-  const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
-  if (own_first)
-    update4<true>(rv, ev, oxa, sv, nv, bv, tv, g.axp[0][0][q], g.axp[0][1][q], g.axp[0][2][q], ay0, ay1, ay2, az0,
-                  az1, az2, omega, om1);
-  else
-    update4<false>(rv, ev, oxa, sv, nv, bv, tv, g.axp[1][0][q], g.axp[1][1][q], g.axp[1][2][q], ay0, ay1, ay2, az0,
-                   az1, az2, omega, om1);
-  *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+  float4 ob = *reinterpret_cast<const float4*>(e_oth + (long long)(k0 - 2) * plane + sj);
+  float4 ox = *reinterpret_cast<const float4*>(e_oth + (long long)(k0 - 1) * plane + sj);
+#pragma unroll
+  for (int kk = 0; kk < kPlanes; ++kk) {
+    const int k = k0 + kk;
+    if (k > d.nz + 1) break;
+    const long long s0 = (long long)(k - 1) * plane + sj;
+    // does this row start (i = 2) with the colour being updated?
+    const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
+    const float4 rr = *reinterpret_cast<const float4*>(r_own + s0);
+    const float4 eo = *reinterpret_cast<const float4*>(e_own + s0);
+    const float4 os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
+    const float4 on = *reinterpret_cast<const float4*>(e_oth + s0 + Lp);
+    const float4 ot = *reinterpret_cast<const float4*>(e_oth + s0 + plane);
+    const float left = e_oth[s0 - 1], right = e_oth[s0 + 4];
+    const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
+    const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+    const float sv[4] = {os.x, os.y, os.z, os.w};
+    const float nv[4] = {on.x, on.y, on.z, on.w};
+    const float bv[4] = {ob.x, ob.y, ob.z, ob.w};
+    const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
+    float ev[4] = {eo.x, eo.y, eo.z, eo.w};
+    const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
+    if (own_first)
+      update4<true>(rv, ev, oxa, sv, nv, bv, tv, g.axp[0][0][q], g.axp[0][1][q], g.axp[0][2][q], ay0, ay1, ay2,
+                    az0, az1, az2, omega, om1);
+    else
+      update4<false>(rv, ev, oxa, sv, nv, bv, tv, g.axp[1][0][q], g.axp[1][1][q], g.axp[1][2][q], ay0, ay1, ay2,
+                     az0, az1, az2, omega, om1);
+    *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+    ob = ox;
+    ox = ot;
+  }
 }
 
 // pc += e at every interior cell, reading e from its colour's packed array, then
@@ -120,7 +132,8 @@ __global__ void k_accumulate_packed(Dims d, double* __restrict__ pc, float* __re
 void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   const Dims& d = c->d;
   const int nq = ((d.nx >> 1) + 3) >> 2;
-  const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)d.nz), block(32, 8);
+  const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)((d.nz + kPlanes - 1) / kPlanes)),
+      block(32, 8);
   if (color == 0)
     k_sor32p<0><<<grid, block, 0, c->st>>>(d, c->g, c->rp[0], c->ep[0], c->ep[1], c->packed_lp, omega, om1);
   else

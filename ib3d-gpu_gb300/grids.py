@@ -241,6 +241,23 @@ def write_gmsh(path, nodes: np.ndarray, tris: np.ndarray) -> None:
         f.write("$EndElements\n")
 
 
+def write_gambit(path, nodes: np.ndarray, tris: np.ndarray) -> None:
+    """Writes a Gambit neutral (.neu) surface mesh in the layout readSurfaceMeshGambit
+    reads (6 header lines, 'NUMNP NELEM NGRPS NBSETS NDFCD NDFVL', 2 lines, 'id x y z',
+    2 lines, 'id type nnodes n1 n2 n3'; subReadInput.f90:187-206)."""
+    with open(path, "w") as f:
+        f.write("        CONTROL INFO 2.4.6\n** GAMBIT NEUTRAL FILE\nsurface\nPROGRAM:                Gambit     VERSION:  2.4.6\n")
+        f.write("generated\n     NUMNP     NELEM     NGRPS    NBSETS     NDFCD     NDFVL\n")
+        f.write(f"{len(nodes):10d}{len(tris):10d}{1:10d}{0:10d}{3:10d}{3:10d}\n")
+        f.write("ENDOFSECTION\n   NODAL COORDINATES 2.4.6\n")
+        for q, (x, y, z) in enumerate(nodes, 1):
+            f.write(f"{q:10d} {x:.17g} {y:.17g} {z:.17g}\n")
+        f.write("ENDOFSECTION\n      ELEMENTS/CELLS 2.4.6\n")
+        for q, (a, b, c) in enumerate(tris, 1):
+            f.write(f"{q:8d} 3  3 {a:8d}{b:8d}{c:8d}\n")
+        f.write("ENDOFSECTION\n")
+
+
 def read_gmsh(path, sur_geo_points: int = 0):
     """Reads a Gmsh 2 ASCII surface mesh as readSurfaceMeshGmsh does
     (subReadInput.f90:143-167): the first `sur_geo_points` element lines are

@@ -40,6 +40,7 @@ extern "C" {
 #define IB3D_ERR_NONFINITE (-6) /* NaN or Inf in a convergence scalar */
 #define IB3D_ERR_MEMORY (-7)    /* device allocation failed */
 #define IB3D_ERR_TOO_LARGE (-8) /* grid larger than ib3d_pressure_solve_noalloc's fixed scratch */
+#define IB3D_ERR_IO (-9)        /* a restart file could not be opened, read or written */
 
 /* SOR stopping test. */
 #define IB3D_CRIT_UPDATE 0   /* max |pc - pco| over fluid cells (subPcorVcor.f90:193-210) */
@@ -57,6 +58,12 @@ extern "C" {
 /* ib3d_params.inner_schedule */
 #define IB3D_INNER_FIXED 0
 #define IB3D_INNER_ADAPTIVE 1
+/* ib3d_params.outlet */
+#define IB3D_OUTLET_ZERO_GRADIENT 0
+#define IB3D_OUTLET_CONVECTIVE 1
+/* ib3d_params.momentum */
+#define IB3D_MOMENTUM_EULER 0
+#define IB3D_MOMENTUM_AB2 1
 
 typedef struct ib3d_params {
   double re;            /* Reynolds number (inputdata line 2; rev = 1/re, subReadInput.f90:22) */
@@ -78,6 +85,12 @@ typedef struct ib3d_params {
                              residual reduction per sweep predicts are needed to reach eps (at most
                              four decades per FP32 solve), so fewer FP64 residual passes run and the
                              last pass overshoots less */
+  int32_t outlet;         /* IB3D_OUTLET_ZERO_GRADIENT (the reference's active outlet,
+                             subBoundaryConditions.f90:149-151) or IB3D_OUTLET_CONVECTIVE (Orlanski,
+                             the commented :153-155, with the speed uc of calculateUc,
+                             subCalculateuc.f90:2-38, taken after each step's pressure forcing) */
+  int32_t momentum;       /* IB3D_MOMENTUM_EULER (nsMomentum) or IB3D_MOMENTUM_AB2: ib3d_step uses
+                             nsMomentumAB (subNavierStokes.f90:1128-1628) after the first step */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
@@ -114,6 +127,20 @@ int ib3d_set_mesh(ib3d_ctx* ctx, int64_t nnodes, const double* xn, const double*
                   int64_t nelems, const int64_t* e1, const int64_t* e2, const int64_t* e3,
                   double xshift, double yshift, double zshift, int64_t inor);
 
+/* ---- Surface-mesh files --------------------------------------------------------
+ * readSurfaceMeshGmsh (subReadInput.f90:137-176, Gmsh 2 ASCII, the first
+ * sur_geo_points element lines skipped) and readSurfaceMeshGambit (:180-213, Gambit
+ * .neu). ib3d_read_surface_mesh returns the counts when any array pointer is NULL,
+ * and fills the arrays (sized by *nnodes, *nelems on entry) otherwise;
+ * ib3d_set_mesh_file reads and calls ib3d_set_mesh. IB3D_ERR_IO on a short or
+ * malformed file. */
+#define IB3D_MESH_GMSH 0
+#define IB3D_MESH_GAMBIT 1
+int ib3d_read_surface_mesh(const char* path, int32_t format, int64_t sur_geo_points, int64_t* nnodes, double* xn,
+                           double* yn, double* zn, int64_t* nelems, int64_t* e1, int64_t* e2, int64_t* e3);
+int ib3d_set_mesh_file(ib3d_ctx* ctx, const char* path, int32_t format, int64_t sur_geo_points, double xshift,
+                       double yshift, double zshift, int64_t inor);
+
 /* Replaces the Poisson coefficient tables that ib3d_create builds as
  * coefficientMatrix does (subCoefficientMatrix.f90:1-59: the 1-D three-point
  * coefficients with the inlet/wall Neumann and outlet Dirichlet rows folded in).
@@ -134,6 +161,14 @@ int ib3d_set_poisson_coefficients(ib3d_ctx* ctx, const double* acx, const double
  * ib3d_search before the next forcing. A context never moved keeps the reference's
  * fixed-body forcing (surface velocity 0, dpdn = 0). */
 int ib3d_move_body(ib3d_ctx* ctx, double dx, double dy, double dz, double us, double vs, double ws);
+
+/* Force-driven motion, shiftSurfaceNodesMovingbody (subSearch.f90:41-76):
+ * u_final = F/(vol*1)*deltat + u_init per axis (vol = pi/6, a unit-diameter sphere of
+ * density 1; u_init the previous call's u_final, 0 before the first), then
+ * ib3d_move_body by u_final*deltat with surface velocity u_final. The reference
+ * never computes Total_Force, so the caller passes the force (e.g. from the drag and
+ * lift of ib3d_stress). vel (may be NULL) receives u_final. */
+int ib3d_move_body_free(ib3d_ctx* ctx, double fx, double fy, double fz, double vel[3]);
 
 /* tagging (subSearch.f90:134-321), cellCount (subSearch.f90:515-596) and
  * computeNormDistance (subSearch.f90:599-678), plus the ghost-point schedule.
@@ -162,6 +197,18 @@ int ib3d_set_field(ib3d_ctx* ctx, int which, const double* in);
 
 /* Per-step routines, in main.f90's order (:46-52). */
 int ib3d_ns_momentum(ib3d_ctx* ctx);      /* nsMomentum, subNavierStokes.f90:622-1122 */
+/* nsMomentumAB (subNavierStokes.f90:1128-1628): nsMomentum's discretisation with the
+ * second-order Adams-Bashforth update ut = u + dt*(0.5*(3*resid - resi_u) + dpdx)
+ * (:1400, 1509, 1619), resi_u the previous call's resid (zero after
+ * ib3d_initial_conditions or an upload, subInitialConditions.f90:24,
+ * subLastConditions.f90:16). Both momentum calls store resid once the arrays exist
+ * (IB3D_MOMENTUM_AB2 in the parameters, or the first call of this function). */
+int ib3d_ns_momentum_ab(ib3d_ctx* ctx);
+/* calculateUc (subCalculateuc.f90:2-38): the outlet convection speed
+ * uc = max(mean ut(nx-4,:,:) over that plane's fluid cells, 0), summed in serial order,
+ * used by the convective outlet; ib3d_step calls it after the pressure forcing when
+ * ib3d_params.outlet is IB3D_OUTLET_CONVECTIVE. uc (may be NULL) receives the value. */
+int ib3d_calculate_uc(ib3d_ctx* ctx, double* uc);
 int ib3d_velocity_bc(ib3d_ctx* ctx);      /* velocityBC, subBoundaryConditions.f90:2-195 */
 int ib3d_solid_cell_bc(ib3d_ctx* ctx);    /* solidCellBC, subBoundaryConditions.f90:199-217 */
 int ib3d_velocity_forcing(ib3d_ctx* ctx); /* velocityForcing1, subForcing.f90:107-652 */
@@ -207,6 +254,22 @@ void* ib3d_stream(ib3d_ctx* ctx);
 void* ib3d_device_field(ib3d_ctx* ctx, int which);
 /* Blocks until the context's stream is idle. */
 int ib3d_synchronize(ib3d_ctx* ctx);
+
+/* ---- Restart files -------------------------------------------------------------
+ * writeResult (subWriteOutput.f90:62-72) saves u, v, w, p and totime, ita, ita1
+ * every 1000 steps as formatted text; lastConditions (subLastConditions.f90:2-42)
+ * reads them back and sets ut = u, vt = v, wt = w. ib3d_write_restart and
+ * ib3d_read_restart do the same straight from and into device memory in a binary
+ * file (64-byte header "IB3DRST1", nx, ny, nz, totime, ita, ita1, nfields = 4, then
+ * u, v, w, p in the Fortran layout), so the driver no longer needs the per-step
+ * download of main.f90:55 to keep a restart. The text pair reads and writes the
+ * reference's own `result` file (one "u v w p totime ita ita1" record per cell, k
+ * outer), for runs that move between the two codes. A file for another grid size
+ * returns IB3D_ERR_ARG; an unreadable or short file IB3D_ERR_IO. */
+int ib3d_write_restart(ib3d_ctx* ctx, const char* path, double totime, int64_t ita, int64_t ita1);
+int ib3d_read_restart(ib3d_ctx* ctx, const char* path, double* totime, int64_t* ita, int64_t* ita1);
+int ib3d_write_result_text(ib3d_ctx* ctx, const char* path, double totime, int64_t ita, int64_t ita1);
+int ib3d_read_result_text(ib3d_ctx* ctx, const char* path, double* totime, int64_t* ita, int64_t* ita1);
 
 /* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A 3-level 3-D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and

@@ -36,6 +36,14 @@ struct OrState {
   double *xnode1, *ynode1, *znode1;
   int64_t *e1, *e2, *e3;
   double *xcent, *ycent, *zcent, *cosA, *cosB, *cosG, *alpha3, *beta3, *gamma3;
+  /* outlet: 0 zero-gradient (the reference's active branch), 1 Orlanski convective
+   * with the convection speed uc of calculateUc (initial value subReadInput.f90:28) */
+  int outlet;
+  double uc;
+  /* nsMomentumAB: resi_u/v/w, the previous momentum call's residual
+   * (allocateArrays, zeroed by initialConditions, subInitialConditions.f90:24) */
+  int momentum;                 /* 0 nsMomentum every step, 1 nsMomentumAB after the first */
+  double *resi_u, *resi_v, *resi_w;
   /* body motion: surface velocity now and one step earlier (0 for a fixed body) */
   int moving;
   double bvel[3], bprev[3];
@@ -75,6 +83,7 @@ OrState* or_create(int64_t nx, int64_t ny, int64_t nz, const double* x1n, const 
   s->rev = 1.0 / re;                       /* :22 */
   s->deltat = deltat;                      /* :24 deltat = dt_order*1e-3 (given directly) */
   s->omega = 1.99; s->eps = 1e-5; s->criterion = 0; s->max_sweeps = 1000000; s->check_every = 1;
+  s->uc = 1.0;                             /* :28 */
   s->x1 = alloc1(nx + 3); s->y1 = alloc1(ny + 3); s->z1 = alloc1(nz + 3);
   s->deltax = alloc1(nx + 2); s->deltay = alloc1(ny + 2); s->deltaz = alloc1(nz + 2);
   s->xu = alloc1(nx + 3); s->yu = alloc1(ny + 2); s->zu = alloc1(nz + 2);
@@ -121,6 +130,9 @@ OrState* or_create(int64_t nx, int64_t ny, int64_t nz, const double* x1n, const 
   double** f[] = {&s->u, &s->v, &s->w, &s->ut, &s->vt, &s->wt, &s->p, &s->pc, &s->pco, &s->b};
   for (size_t q = 0; q < sizeof(f) / sizeof(f[0]); ++q) *f[q] = (double*)calloc((size_t)n3, sizeof(double));
   s->cell = (int64_t*)calloc((size_t)n3, sizeof(int64_t));
+  s->resi_u = (double*)calloc((size_t)n3, sizeof(double));
+  s->resi_v = (double*)calloc((size_t)n3, sizeof(double));
+  s->resi_w = (double*)calloc((size_t)n3, sizeof(double));
   s->minElemcell = (int64_t*)calloc((size_t)n3, sizeof(int64_t));
   s->Acx = (double*)calloc((size_t)(3 * nx), sizeof(double));
   s->Acy = (double*)calloc((size_t)(3 * ny), sizeof(double));
@@ -151,6 +163,7 @@ void or_destroy(OrState* s) {
   for (int q = 0; q < 5; ++q) free(s->scache[q]);
   free(s->cell); free(s->minElemcell); free(s->e1); free(s->e2); free(s->e3);
   free(s->fluid); free(s->solid); free(s->ib); free(s->red); free(s->black); free(s->nelp);
+  free(s->resi_u); free(s->resi_v); free(s->resi_w);
   free(s);
 }
 
@@ -236,6 +249,23 @@ void or_set_coefficients(OrState* s, const double* acx, const double* acy, const
   memcpy(s->Acx, acx, (size_t)(3 * s->nx) * sizeof(double));
   memcpy(s->Acy, acy, (size_t)(3 * s->ny) * sizeof(double));
   memcpy(s->Acz, acz, (size_t)(3 * s->nz) * sizeof(double));
+}
+
+/* shiftSurfaceNodesMovingbody (subSearch.f90:41-76) with the force given:
+ * vol = (pi*(1.0)**3)/6. (:53, pi = 4*atan(1), subReadInput.f90:23),
+ * u_final = (F/(vol*1.))*deltat + u_init, move = u_final*deltat. */
+int or_move_body_free(OrState* s, double fx, double fy, double fz, double vel[3]) {
+  const double pi = 4.0 * atan(1.0);
+  const double vol = (pi * (1.0 * 1.0 * 1.0)) / 6.0;
+  const double f[3] = {fx, fy, fz};
+  double v[3];
+  for (int q = 0; q < 3; ++q) {
+    const double init = s->moving ? s->bvel[q] : 0.0;
+    v[q] = (f[q] / (vol * 1.0)) * s->deltat + init;
+  }
+  const int rc = or_move_body(s, v[0] * s->deltat, v[1] * s->deltat, v[2] * s->deltat, v[0], v[1], v[2]);
+  if (vel) { vel[0] = v[0]; vel[1] = v[1]; vel[2] = v[2]; }
+  return rc;
 }
 
 /* Signed distance of a corner to the plane of element m (subSearch.f90:204-234). */
@@ -362,8 +392,8 @@ int or_search(OrState* s, const int64_t box[6]) {
 /* initialConditions (subInitialConditions.f90:2-48). */
 void or_initial_conditions(OrState* s) {
   const int64_t n3 = NX2 * NY2 * (s->nz + 2);
-  double* f[] = {s->u, s->ut, s->v, s->vt, s->w, s->wt, s->p};
-  for (int q = 0; q < 7; ++q) memset(f[q], 0, (size_t)n3 * sizeof(double));
+  double* f[] = {s->u, s->ut, s->v, s->vt, s->w, s->wt, s->p, s->resi_u, s->resi_v, s->resi_w};
+  for (int q = 0; q < 10; ++q) memset(f[q], 0, (size_t)n3 * sizeof(double));   /* :19-24 */
   for (int64_t n = 1; n <= s->nfluid; ++n) {
     int64_t i = L(s->fluid, s->nfluid, n, 1), j = L(s->fluid, s->nfluid, n, 2), k = L(s->fluid, s->nfluid, n, 3);
     F3(s->u, i, j, k) = 1.0;
@@ -490,6 +520,14 @@ void or_non_uni_coeff(OrState* s) {
   }
 }
 
+/* nsMomentum (subNavierStokes.f90:622-1122) and nsMomentumAB (1128-1628): the same
+ * discretisation, Euler or second-order Adams-Bashforth update (:1400, 1509, 1619);
+ * both store resid in resi_* (:897, 1006, 1115 and 1403, 1512, 1622). */
+static void ns_momentum(OrState* s, int ab2);
+void or_ns_momentum(OrState* s) { ns_momentum(s, 0); }
+void or_ns_momentum_ab(OrState* s) { ns_momentum(s, 1); }
+void or_set_momentum(OrState* s, int momentum) { s->momentum = momentum; }
+
 /* velocityBC active branch (subBoundaryConditions.f90:350-406). */
 void or_velocity_bc(OrState* s) {
   const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
@@ -498,9 +536,19 @@ void or_velocity_bc(OrState* s) {
       F3(s->ut, 1, j, k) = 1.0;
       F3(s->vt, 1, j, k) = -F3(s->vt, 2, j, k);
       F3(s->wt, 1, j, k) = -F3(s->wt, 2, j, k);
-      F3(s->ut, nx + 1, j, k) = F3(s->ut, nx, j, k);
-      F3(s->vt, nx + 2, j, k) = F3(s->vt, nx + 1, j, k);
-      F3(s->wt, nx + 2, j, k) = F3(s->wt, nx + 1, j, k);
+      if (s->outlet == 1) {        /* Orlanski: the commented lines :153-155 (active at :131-133) */
+        const double uc = s->uc, dt = s->deltat;
+        F3(s->ut, nx + 1, j, k) = F3(s->u, nx + 1, j, k) - (dt / s->deltax[nx + 1]) * uc *
+                                  (F3(s->u, nx + 1, j, k) - F3(s->u, nx, j, k));
+        F3(s->vt, nx + 2, j, k) = -F3(s->vt, nx + 1, j, k) + F3(s->v, nx + 2, j, k) + F3(s->v, nx + 1, j, k) -
+                                  (2.0 * dt / s->deltax[nx + 2]) * uc * (F3(s->v, nx + 2, j, k) - F3(s->v, nx + 1, j, k));
+        F3(s->wt, nx + 2, j, k) = -F3(s->wt, nx + 1, j, k) + F3(s->w, nx + 2, j, k) + F3(s->w, nx + 1, j, k) -
+                                  (2.0 * dt / s->deltax[nx + 2]) * uc * (F3(s->w, nx + 2, j, k) - F3(s->w, nx + 1, j, k));
+      } else {                                                    /* zero gradient, :149-151 */
+        F3(s->ut, nx + 1, j, k) = F3(s->ut, nx, j, k);
+        F3(s->vt, nx + 2, j, k) = F3(s->vt, nx + 1, j, k);
+        F3(s->wt, nx + 2, j, k) = F3(s->wt, nx + 1, j, k);
+      }
     }
   for (int64_t k = 2; k <= nz + 1; ++k)
     for (int64_t i = 2; i <= nx + 1; ++i) {
@@ -549,7 +597,7 @@ static inline double up1(double adv, double dA, double r, double qm, double q0, 
 }
 
 /* nsMomentum (subNavierStokes.f90:622-1122): explicit Euler predictor per fluid cell. */
-void or_ns_momentum(OrState* s) {
+static void ns_momentum(OrState* s, int ab2) {
   const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
   const double rev = s->rev, deltat = s->deltat;
   const double *DX = s->deltax, *DY = s->deltay, *DZ = s->deltaz;
@@ -616,7 +664,9 @@ void or_ns_momentum(OrState* s) {
       double d2z = (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-u12 / (0.5 * dz2zt)) + (u10 / (0.5 * dz2zb)));
       double xtt2 = rev * (d2x + d2y + d2z);
       double resid = -cx - cy - cz + xtt2;
-      F3(s->ut, i, j, k) = u0 + deltat * (resid + dpdx);
+      if (ab2) F3(s->ut, i, j, k) = u0 + deltat * (0.5 * (3.0 * resid - F3(s->resi_u, i, j, k)) + dpdx);
+      else F3(s->ut, i, j, k) = u0 + deltat * (resid + dpdx);
+      F3(s->resi_u, i, j, k) = resid;                               /* :897 (1403) */
     }
     /* ---- v momentum (:901-1006) ---- */
     {
@@ -643,7 +693,9 @@ void or_ns_momentum(OrState* s) {
       double d2z = (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-v14 / (0.5 * dz2zt)) + (v12 / (0.5 * dz2zb)));
       double ytt2 = rev * (d2x + d2y + d2z);
       double resid = -cx - cy - cz + ytt2;
-      F3(s->vt, i, j, k) = v0 + deltat * (resid + dpdy);
+      if (ab2) F3(s->vt, i, j, k) = v0 + deltat * (0.5 * (3.0 * resid - F3(s->resi_v, i, j, k)) + dpdy);
+      else F3(s->vt, i, j, k) = v0 + deltat * (resid + dpdy);
+      F3(s->resi_v, i, j, k) = resid;                               /* :897 (1403) */
     }
     /* ---- w momentum (:1010-1116) ---- */
     {
@@ -670,7 +722,9 @@ void or_ns_momentum(OrState* s) {
       double d2z = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
       double ztt2 = rev * (d2x + d2y + d2z);
       double resid = -cx - cy - cz + ztt2;
-      F3(s->wt, i, j, k) = w0 + deltat * (resid + dpdz);
+      if (ab2) F3(s->wt, i, j, k) = w0 + deltat * (0.5 * (3.0 * resid - F3(s->resi_w, i, j, k)) + dpdz);
+      else F3(s->wt, i, j, k) = w0 + deltat * (resid + dpdz);
+      F3(s->resi_w, i, j, k) = resid;                               /* :897 (1403) */
     }
   }
 }
@@ -816,6 +870,25 @@ int or_pressure_forcing(OrState* s) {
   }
   return 0;
 }
+
+/* calculateUc (subCalculateuc.f90:2-38): uc = max(mean of ut(nx-4,j,k) over the
+ * fluid cells of that plane, 0), summed serially k outer, j inner. */
+void or_calculate_uc(OrState* s) {
+  const int64_t i = s->nx - 4;
+  double uc1 = 0.0;
+  int64_t count = 0;
+  for (int64_t k = 2; k <= s->nz + 1; ++k)
+    for (int64_t j = 2; j <= s->ny + 1; ++j)
+      if (F3(s->cell, i, j, k) == 0) {
+        uc1 = uc1 + F3(s->ut, i, j, k);
+        count = count + 1;
+      }
+  uc1 = uc1 / (double)count;
+  s->uc = uc1 > 0.0 ? uc1 : 0.0;   /* dmax1(uc1, uc0) */
+}
+
+void or_set_outlet(OrState* s, int outlet) { s->outlet = outlet; }
+double or_uc(const OrState* s) { return s->uc; }
 
 /* Residual of the pressure-correction system at one fluid cell:
  * b/dt - sum(A_nb pc_nb) - diag pc, in the order the SOR numerator uses. */
@@ -1062,7 +1135,8 @@ int or_stress(OrState* s, int first, double coef[4]) {
 
 /* One time step in main.f90's order (:42-66; step 1 at :26-39). */
 int or_step(OrState* s, int first, int64_t* nsweeps, double coef[4]) {
-  or_ns_momentum(s);
+  if (s->momentum == 1 && !first) or_ns_momentum_ab(s);        /* main.f90:45 */
+  else or_ns_momentum(s);                                      /* main.f90:46 (30) */
   or_velocity_bc(s);
   or_solid_cell_bc(s);
   int rc = or_velocity_forcing(s);
@@ -1072,6 +1146,7 @@ int or_step(OrState* s, int first, int64_t* nsweeps, double coef[4]) {
   int nc = or_poisson_solver(s, nsweeps, &divmax, &dss, &err);
   rc = or_pressure_forcing(s);
   if (rc) return rc;
+  if (s->outlet == 1) or_calculate_uc(s);                       /* main.f90:53-54 hook */
   rc = or_stress(s, first, coef);
   if (rc) return rc;
   return nc;

@@ -53,6 +53,10 @@ int or_set_mesh(OrState* s, int64_t nnodes, const double* xn, const double* yn, 
  * or_search afterwards. */
 int or_move_body(OrState* s, double dx, double dy, double dz, double us, double vs, double ws);
 
+/* Force-driven motion (shiftSurfaceNodesMovingbody, subSearch.f90:41-76) with the
+ * surface force given: the body velocity integrates F/(pi/6) over deltat. */
+int or_move_body_free(OrState* s, double fx, double fy, double fz, double vel[3]);
+
 /* tagging (subSearch.f90:134-321) + cellCount (515-596) + computeNormDistance (599-678).
  * box = {i_start, i_end, j_start, j_end, k_start, k_end} (1-based, inclusive). */
 int or_search(OrState* s, const int64_t box[6]);
@@ -69,6 +73,9 @@ void or_set_coefficients(OrState* s, const double* acx, const double* acy, const
 
 /* Per-step routines (main.f90:29-39 and 42-66). */
 void or_ns_momentum(OrState* s);                        /* subNavierStokes.f90:622-1122 */
+void or_ns_momentum_ab(OrState* s);                     /* nsMomentumAB, subNavierStokes.f90:1128-1628 */
+/* 0: or_step uses nsMomentum every step; 1: nsMomentumAB after the first step. */
+void or_set_momentum(OrState* s, int momentum);
 void or_velocity_bc(OrState* s);                        /* subBoundaryConditions.f90:2-195 (active branch) */
 void or_solid_cell_bc(OrState* s);                      /* subBoundaryConditions.f90:199-217 */
 int or_velocity_forcing(OrState* s);                    /* subForcing.f90:107-652 */
@@ -79,6 +86,13 @@ int or_stress(OrState* s, int first, double coef[4]);   /* subStressCal1/2.f90 *
 /* REDBLACKSOR alone (subPcorVcor.f90:148-212) on the b set by the caller (field 8),
  * pc starting from 0. */
 int or_redblack_sor(OrState* s, int64_t* nsweeps, double* final_err);
+/* Outlet of velocityBC: 0 zero-gradient (subBoundaryConditions.f90:149-151, the
+ * reference's active branch), 1 Orlanski convective (:153-155) with the speed uc that
+ * or_calculate_uc (calculateUc, subCalculateuc.f90:2-38) sets after each step's
+ * pressure forcing; uc starts at 1 (subReadInput.f90:28). */
+void or_set_outlet(OrState* s, int outlet);
+void or_calculate_uc(OrState* s);
+double or_uc(const OrState* s);
 /* One full time step as main.f90:42-66 sequences it; first selects stressCal1. */
 int or_step(OrState* s, int first, int64_t* nsweeps, double coef[4]);
 

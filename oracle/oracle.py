@@ -44,9 +44,15 @@ def lib() -> C.CDLL:
         "or_coefficient_matrix": (None, [_VP]),
         "or_set_coefficients": (None, [_VP, _D, _D, _D]),
         "or_no_body": (None, [_VP]),
+        "or_move_body_free": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _D]),
         "or_redblack_sor": (C.c_int, [_VP, _I64, _D]),
         "or_non_uni_coeff": (None, [_VP]),
         "or_ns_momentum": (None, [_VP]),
+        "or_ns_momentum_ab": (None, [_VP]),
+        "or_set_momentum": (None, [_VP, C.c_int]),
+        "or_set_outlet": (None, [_VP, C.c_int]),
+        "or_calculate_uc": (None, [_VP]),
+        "or_uc": (C.c_double, [_VP]),
         "or_velocity_bc": (None, [_VP]),
         "or_solid_cell_bc": (None, [_VP]),
         "or_velocity_forcing": (C.c_int, [_VP]),
@@ -88,7 +94,8 @@ class Oracle:
     """Serial FP64 restatement of the reference's hot path on one grid."""
 
     def __init__(self, x, y, z, re: float, deltat: float, omega: float = 1.99, eps: float = 1e-5,
-                 criterion: int = 0, max_sweeps: int = 1_000_000, check_every: int = 1):
+                 criterion: int = 0, max_sweeps: int = 1_000_000, check_every: int = 1, outlet: int = 0,
+                 momentum: int = 0):
         self.L = lib()
         self.x = np.ascontiguousarray(x, dtype=np.float64)
         self.y = np.ascontiguousarray(y, dtype=np.float64)
@@ -98,6 +105,8 @@ class Oracle:
         self._h = self.L.or_create(self.nx, self.ny, self.nz, self.x.ctypes.data_as(_D), self.y.ctypes.data_as(_D),
                                    self.z.ctypes.data_as(_D), float(re), float(deltat))
         self.set_solver(omega, eps, criterion, max_sweeps, check_every)
+        self.L.or_set_outlet(self._h, int(outlet))
+        self.L.or_set_momentum(self._h, int(momentum))
         self.L.or_coefficient_matrix(self._h)
         self.L.or_non_uni_coeff(self._h)
         self.nelems = 0
@@ -131,6 +140,11 @@ class Oracle:
                                      e2.ctypes.data_as(_I64), e3.ctypes.data_as(_I64), float(shift[0]),
                                      float(shift[1]), float(shift[2]), int(inor)), "or_set_mesh")
         self.nelems = len(tris)
+
+    def move_body_free(self, fx, fy, fz) -> np.ndarray:
+        v = np.zeros(3)
+        self._chk(self.L.or_move_body_free(self._h, fx, fy, fz, v.ctypes.data_as(_D)), "or_move_body_free")
+        return v
 
     def no_body(self):
         """Every interior cell fluid (no surface mesh, no search)."""
@@ -223,6 +237,17 @@ class Oracle:
         if rc and not allow_noconv:
             raise OracleError(rc, "or_poisson_solver")
         return {"sweeps": int(ns[0]), "divmax": vals[0], "derr_std_st": vals[1], "final_err": vals[2], "rc": rc}
+
+    def ns_momentum_ab(self):
+        self.L.or_ns_momentum_ab(self._h)
+
+    def calculate_uc(self) -> float:
+        self.L.or_calculate_uc(self._h)
+        return float(self.L.or_uc(self._h))
+
+    @property
+    def uc(self) -> float:
+        return float(self.L.or_uc(self._h))
 
     def redblack_sor(self, allow_noconv: bool = False) -> dict:
         ns = np.zeros(1, np.int64)

@@ -6,6 +6,7 @@ from __future__ import annotations
 import ctypes
 import pathlib
 
+import numpy as np
 import pytest
 
 
@@ -38,9 +39,10 @@ def test_python_mirror_binds_every_symbol(ib3d, built_lib):
 
 def test_params_struct_layout(ib3d, built_lib):
     p = ib3d.default_params()
-    # 4 doubles, int64, 6 int32, double, int32 + 4 bytes of tail padding
-    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8 + 8
+    # 4 doubles, int64, 6 int32, double, 3 int32 + 4 bytes of tail padding
+    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8 + 3 * 4 + 4
     assert ib3d.Params.omega_inner.offset == 64 and ib3d.Params.inner_schedule.offset == 72
+    assert ib3d.Params.outlet.offset == 76 and ib3d.Params.momentum.offset == 80
     assert ctypes.sizeof(ib3d.SolveStats) == 7 * 8
     assert p.omega == 1.99 and p.eps == 1e-5 and p.criterion == ib3d.CRIT_UPDATE
     assert p.inner_schedule == ib3d.INNER_FIXED
@@ -60,3 +62,26 @@ def test_oracle_library_builds_and_loads(oracle_mod):
     L = oracle_mod.lib()
     for n in ("or_create", "or_step", "or_search", "or_poisson_solver", "or_stress"):
         assert hasattr(L, n)
+
+
+@pytest.mark.parametrize("fmt", ["gmsh", "gambit"])
+def test_surface_mesh_files_round_trip(ib3d, built_lib, grids, tmp_path, fmt):
+    """ib3d_read_surface_mesh (host code, no GPU) reads back what grids writes in the
+    record layout of readSurfaceMeshGmsh / readSurfaceMeshGambit, exactly."""
+    nodes, tris = grids.icosphere(3, 0.5)
+    path = tmp_path / f"body.{fmt}"
+    if fmt == "gmsh":
+        grids.write_gmsh(path, nodes, tris)
+        got_n, got_t = ib3d.read_surface_mesh(path, ib3d.MESH_GMSH)
+    else:
+        grids.write_gambit(path, nodes, tris)
+        got_n, got_t = ib3d.read_surface_mesh(path, ib3d.MESH_GAMBIT)
+    assert np.array_equal(got_n, nodes) and np.array_equal(got_t, tris)
+    # surGeoPoints: the first element lines are skipped
+    if fmt == "gmsh":
+        _, t2 = ib3d.read_surface_mesh(path, ib3d.MESH_GMSH, sur_geo_points=5)
+        assert np.array_equal(t2, tris[5:])
+    with pytest.raises(ib3d.IB3DError) as e:
+        path.write_text(path.read_text()[:200])
+        ib3d.read_surface_mesh(path, ib3d.MESH_GMSH if fmt == "gmsh" else ib3d.MESH_GAMBIT)
+    assert e.value.code == ib3d.ERR_IO

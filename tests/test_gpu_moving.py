@@ -59,3 +59,38 @@ def test_step_requires_search_after_move(ib3d, grids):
     s.search(cs.box)
     s.step(True)
     s.close()
+
+
+def test_force_driven_motion_bit_exact(ib3d, oracle_mod, grids):
+    """shiftSurfaceNodesMovingbody: the body velocity integrates the given force
+    (density 1, unit-diameter sphere); the GPU and the oracle move, re-tag and step
+    identically."""
+    cs = grids.case("tiny")
+    s, o = _pair(ib3d, oracle_mod, cs)
+    for step in range(1, 5):
+        force = (0.0, 40.0 * (-1) ** step, 5.0)
+        vg = s.move_body_free(*force)
+        vo = o.move_body_free(*force)
+        assert np.array_equal(vg, vo)
+        assert s.search(cs.box) == o.search(cs.box)
+        gst, gcoef = s.step(step == 1)
+        ost, ocoef = o.step(step == 1)
+        assert gst["sweeps"] == ost["sweeps"] and np.array_equal(gcoef, ocoef), step
+    for f in FIELDS:
+        _same(s.get_field(f), o.get_field(f), f"after force-driven steps {f}")
+    s.close()
+
+
+def test_mesh_file_gives_the_same_search(ib3d, grids, tmp_path):
+    cs = grids.case("tiny")
+    nodes, tris = grids.icosphere(cs.subdivisions, cs.radius)
+    a = ib3d.setup_case(cs)
+    for fmt, writer in ((ib3d.MESH_GMSH, grids.write_gmsh), (ib3d.MESH_GAMBIT, grids.write_gambit)):
+        path = tmp_path / f"body{fmt}"
+        writer(path, nodes, tris)
+        b = ib3d.Solver(cs.x, cs.y, cs.z, ib3d.default_params(re=cs.re, deltat=cs.dt))
+        b.set_mesh_file(path, fmt)
+        assert b.search(cs.box) == a.counts
+        assert np.array_equal(b.get_search()["cell"], a.get_search()["cell"])
+        b.close()
+    a.close()

@@ -18,7 +18,8 @@ FIELDS = ("u", "v", "w", "ut", "vt", "wt", "p")
 
 def _pair(ib3d, oracle_mod, cs, **kw):
     o = oracle_mod.setup_case(cs, **{k: v for k, v in kw.items() if k in ("criterion", "eps", "max_sweeps",
-                                                                           "check_every", "omega")})
+                                                                           "check_every", "omega", "outlet",
+                                                                           "momentum")})
     s = ib3d.setup_case(cs, **kw)
     return s, o
 
@@ -240,3 +241,37 @@ def test_download_matches_get_field(ib3d, grids):
     for f in FIELDS:
         _same(d[f], s.get_field(f), f)
     s.close()
+
+
+@pytest.mark.parametrize("outlet,momentum", [(1, 0), (0, 1), (1, 1)])
+def test_convective_outlet_and_ab2_steps_bit_exact(ib3d, oracle_mod, grids, outlet, momentum):
+    """The reference's optional branches: Orlanski outlet with calculateUc after each
+    step (subBoundaryConditions.f90:153-155, subCalculateuc.f90:2-38) and the
+    Adams-Bashforth predictor nsMomentumAB after the first step
+    (subNavierStokes.f90:1128-1628), whole steps bit for bit."""
+    cs = grids.case("small")
+    s, o = _pair(ib3d, oracle_mod, cs, outlet=outlet, momentum=momentum)
+    for step in range(1, 5):
+        gst, gcoef = s.step(step == 1)
+        ost, ocoef = o.step(step == 1)
+        assert gst["sweeps"] == ost["sweeps"], step
+        assert np.array_equal(gcoef, ocoef), (step, gcoef, ocoef)
+    for f in FIELDS:
+        _same(s.get_field(f), o.get_field(f), f"outlet {outlet} momentum {momentum}: {f}")
+    if outlet:
+        assert s.calculate_uc() == o.calculate_uc()
+    s.close()
+
+
+def test_ab2_differs_from_euler_after_the_first_step(ib3d, grids):
+    cs = grids.case("tiny")
+    e = ib3d.setup_case(cs)
+    a = ib3d.setup_case(cs, momentum=ib3d.MOMENTUM_AB2)
+    for step in (1, 2):
+        e.step(step == 1)
+        a.step(step == 1)
+        if step == 1:
+            assert np.array_equal(e.get_field("u"), a.get_field("u"))
+    assert not np.array_equal(e.get_field("u"), a.get_field("u"))
+    e.close()
+    a.close()

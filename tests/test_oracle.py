@@ -208,3 +208,18 @@ def test_neumann_coefficients_and_standalone_sor(oracle_mod, grids):
     import importlib
     res = importlib.import_module("test_gpu_poisson").residual
     assert res(P, o.get_field("pc")) < 1e-8
+
+
+def test_calculate_uc_and_ab2_known_answers(oracle_mod, grids):
+    """calculateUc of uniform flow u = 1 is 1 (the mean over the fluid cells of plane
+    nx-4); nsMomentumAB with resi = resid of the same fields equals the Euler update
+    (0.5*(3r - r) = r), and with resi = 0 it is the Euler update with 1.5 r."""
+    cs = grids.case("tiny")
+    o = oracle_mod.setup_case(cs)
+    o.set_field("ut", o.get_field("u"))
+    assert o.calculate_uc() == 1.0
+    p = oracle_mod.setup_case(cs)
+    p.ns_momentum()
+    ut_euler = p.get_field("ut")
+    p.ns_momentum_ab()                       # resi now holds this state's resid
+    assert np.allclose(p.get_field("ut"), ut_euler, rtol=0, atol=1e-13)
