@@ -102,15 +102,17 @@ def load_net(pkg, path=WEIGHTS):
 
 
 def train_net(pkg, cs, out: str, seconds: float) -> dict:
-    """Generates snapshots (4 perturbed runs at Re 200/250/300/350, 24 steps, 16 random
-    64^3 patches per step from step 3), trains with Adam for `seconds` (batch 8, lr 1e-3
-    then 2e-4 for the last 30 %) and writes the FP32 weights."""
+    """Generates snapshots (4 perturbed runs at Re 200/250/300/350, 24 steps, 8 random
+    patches of 64^3 coarse voxels = 128^3 cells per step from step 3), trains with Adam
+    for `seconds` (batch 8, lr 1e-3 then 2e-4 for the last 30 %), writes the FP32
+    weights, and compares sweeps on a held-out Re 275 run (adaptive pass lengths, so
+    that the counts resolve differences below 256 sweeps)."""
     import dataclasses
     import numpy as np
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
     net = pkg.Net(seed=0)
-    net.reserve(64, 4 * 24 * 16)
-    gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 16)
+    net.reserve(64, 4 * 24 * 8)
+    gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 8)
     fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
     before = fit()
     t0, steps = time.perf_counter(), 0
@@ -121,10 +123,11 @@ def train_net(pkg, cs, out: str, seconds: float) -> dict:
     after = fit()
     pathlib.Path(out).parent.mkdir(parents=True, exist_ok=True)
     net.get_params().astype("<f4").tofile(out)
-    ev = learned.evaluate(net, dataclasses.replace(cs), 275.0, 12)
+    ev = learned.evaluate(net, dataclasses.replace(cs), 275.0, 12, inner_schedule=1)
     return {"weights": str(out), "patches": gen["patches"], "generate_s": gen["seconds"], "adam_steps": steps,
             "train_s": time.perf_counter() - t0, "training_set_loss": [before, after],
-            "eval_re275": {k: {"sweeps": v["sweeps"], "seconds": v["seconds"]} for k, v in ev.items()}}
+            "eval_re275": {k: {"sweeps": v["sweeps"], "seconds": v["seconds"], "initial_err": v["initial_err"]}
+                           for k, v in ev.items()}}
 
 
 # ------------------------------------------------------------------ clocks
@@ -245,10 +248,12 @@ def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bo
     return {"seconds": t, "stats": stats, "coef": list(map(float, coef)), "timers": tm, "clocks": clk}
 
 
-def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist):
-    """The fast form through the C ABI with pinned host buffers in the timed region."""
+def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None):
+    """The headline form through the C ABI with pinned host buffers in the timed region."""
     import torch
     s = pkg.setup_case(cs, **mode)
+    if net is not None:
+        s.attach_net(net)
     first = True
     for _ in range(warmup):
         s.step(first)
@@ -357,6 +362,43 @@ def run_poisson(pkg, n: int) -> dict:
     return out
 
 
+def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, freq: float = 0.2) -> dict:
+    """The body oscillates as y(t) = amp sin(2 pi freq t): before every step the nodes
+    move (ib3d_move_body, surface velocity y'(t)), the search re-tags a box around
+    the new position, then the step runs. Timed with CUDA events on the library
+    stream around the timed steps (move, search and step together)."""
+    import math
+    import torch
+    s = pkg.setup_case(cs, **mode)
+    w = 2.0 * math.pi * freq
+    y = 0.0
+    stream = torch.cuda.ExternalStream(s.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sweeps, coef, t_search = [], None, 0.0
+    for n in range(1, warmup + steps + 1):
+        if n == warmup + 1:
+            s.synchronize()
+            e0.record(stream)
+        t = n * cs.dt
+        yn = amp * math.sin(w * t)
+        s.move_body(0.0, yn - y, 0.0, 0.0, amp * w * math.cos(w * t), 0.0)
+        y = yn
+        t0 = time.perf_counter()
+        s.search(pkg.grids.body_box(cs, (0.0, y, 0.0)))
+        if n > warmup:
+            t_search += time.perf_counter() - t0
+        st, coef = s.step(n == 1)
+        if n > warmup:
+            sweeps.append(st["sweeps"])
+    e1.record(stream)
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    s.close()
+    return {"value": steps / sec, "unit": "steps/s", "ms_per_step": 1e3 * sec / steps,
+            "sweeps_per_step": sum(sweeps) / len(sweeps), "search_ms_per_step": 1e3 * t_search / steps,
+            "drag_lift": list(map(float, coef)), "y_end": y}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -376,6 +418,10 @@ def main():
                     help="instead of the benchmark: generate snapshots, train the warm-start U-Net and write "
                          "its weights to this file")
     ap.add_argument("--train-seconds", type=float, default=300.0)
+    ap.add_argument("--moving", action="store_true",
+                    help="instead of the step benchmark: the transversely oscillating sphere "
+                         "(y = 0.2 sin(2 pi 0.2 t), search every step) on --case (default sphere384), "
+                         "FP32 form and plain FP64")
     ap.add_argument("--set", default="",
                     help="comma-separated key=value overrides of the FP32-sweep arm's solver parameters")
     ap.add_argument("--arms", default="fast,learned,plain,e2e,cpu",
@@ -391,6 +437,17 @@ def main():
         if dist.rank == 0:
             print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds)),
                   flush=True)
+        dist.close()
+        return
+    if args.moving:
+        if dist.rank == 0:
+            mcs = workload(pkg, args.case if args.case != "sphere256" else "sphere384")
+            out = {"workload": f"{mcs.name} {mcs.shape[0]}x{mcs.shape[1]}x{mcs.shape[2]}, Re {mcs.re:g}, moving sphere "
+                               "y = 0.2 sin(2 pi 0.2 t), search every step, residual <= 1e-6",
+                   "fp32": run_moving(pkg, mcs, FAST, warmup, args.steps),
+                   "plain_fp64": run_moving(pkg, mcs, PLAIN, warmup, max(1, args.plain_steps // 2))}
+            out["speedup"] = out["fp32"]["value"] / out["plain_fp64"]["value"]
+            print(json.dumps(out), flush=True)
         dist.close()
         return
     if args.poisson:
@@ -439,8 +496,13 @@ def main():
         print(json.dumps({"recorded": str(path), "sweeps": counts}), flush=True)
         return
 
+    arms = set(args.arms.split(","))
+    # Headline: FP32 sweeps in FP64 defect correction with the learned warm start (the
+    # trained network in the package); without weights, the previous-correction warm start.
+    net = load_net(pkg) if "learned" in arms else None
+    head_mode = dict(FAST, warm_start=pkg.WARM_LEARNED) if net is not None else FAST
     clocks = Clocks(dist.local)
-    fast = run_arm(pkg, cs, FAST, warmup, args.steps, dist, timers=True, clocks=clocks)
+    fast = run_arm(pkg, cs, head_mode, warmup, args.steps, dist, timers=True, clocks=clocks, net=net)
     t = dist.max(fast["seconds"])
     value = dist.world * args.steps / t
     tm = fast["timers"]
@@ -452,21 +514,14 @@ def main():
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     phase_total = sum(tm[f"{p}_ms"] for p in pkg.Timers.PHASES)
 
-    arms = set(args.arms.split(","))
-    learned_line = None
-    net = load_net(pkg) if "learned" in arms else None
-    if net is not None:
-        lmode = dict(FAST, warm_start=pkg.WARM_LEARNED)
-        lrn = run_arm(pkg, cs, lmode, warmup, args.steps, dist, timers=True, net=net)
-        lt = dist.max(lrn["seconds"])
-        ltm = lrn["timers"]
-        lsweeps = sum(st["sweeps"] for st in lrn["stats"]) / args.steps
-        learned_line = {"value": dist.world * args.steps / lt, "unit": "steps/s",
-                        "ms_per_step": 1e3 * lt / args.steps, "sweeps_per_step": lsweeps,
-                        "sweeps_saved_vs_previous_correction": 1.0 - lsweeps / (sweeps / args.steps),
-                        "net_ms_per_step": ltm["net_ms"] / args.steps,
-                        "drag_lift": lrn["coef"], "weights": str(WEIGHTS.relative_to(ROOT))}
-        net.close()
+    prev_line = None
+    if net is not None and "fast" in arms:
+        prv = run_arm(pkg, cs, FAST, warmup, args.steps, dist, timers=True)
+        pt = dist.max(prv["seconds"])
+        psweeps = sum(st["sweeps"] for st in prv["stats"]) / args.steps
+        prev_line = {"value": dist.world * args.steps / pt, "unit": "steps/s", "ms_per_step": 1e3 * pt / args.steps,
+                     "sweeps_per_step": psweeps, "drag_lift": prv["coef"],
+                     "learned_sweeps_saved": 1.0 - (sweeps / args.steps) / psweeps}
     plain_steps = max(1, min(args.plain_steps, args.steps))
     if "plain" in arms:
         plain = run_arm(pkg, cs, PLAIN, warmup, plain_steps, dist, timers=True)
@@ -481,7 +536,7 @@ def main():
         plain_sweeps = table[warmup:warmup + plain_steps] or [0]
 
     if "e2e" in arms:
-        e2e = run_e2e(pkg, cs, FAST, warmup, args.steps, dist)
+        e2e = run_e2e(pkg, cs, head_mode, warmup, args.steps, dist, net=net)
         e2e_value = dist.world * args.steps / dist.max(e2e["seconds"])
     else:
         e2e, e2e_value = {"h2d": None, "d2h": None}, None
@@ -494,8 +549,10 @@ def main():
         "config": {"workload": f"{cs.name}: {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]} non-uniform grid, sphere D=1, "
                                f"Re {cs.re:g}, dt {cs.dt:g}, red-black SOR omega {cs.omega:g} to FP64 residual "
                                f"L-inf <= {cs.eps:g}",
-                   "mode": "FP32 red-black sweeps inside FP64 defect correction, warm start from the previous "
-                           "step's correction, inner relaxation 1.994 (learned warm start not in this line)",
+                   "mode": ("FP32 red-black sweeps inside FP64 defect correction, inner relaxation 1.994, "
+                            + ("learned warm start (BF16 U-Net on the 2x2x2-coarsened domain, weights "
+                               f"{WEIGHTS.relative_to(ROOT)})" if net is not None
+                               else "warm start from the previous step's correction")),
                    "inner_sweeps": FAST["inner_sweeps"],
                    "l2": "inputs larger than L2: each step reads/writes 7 FP64 fields of 77.7 MB",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
@@ -504,9 +561,8 @@ def main():
                        "ms_per_sweep": t_sweep64 * 1e3 if t_sweep64 else None,
                        "sweep_bound": "FP64 ALU (GB300 FP64 ~0.5 TFMA/s measured)"},
         "speedup_vs_plain_fp64": value / plain_value if plain_value else None,
-        "learned_fp32": learned_line,
-        "learned_speedup_vs_plain_fp64": (learned_line["value"] / plain_value
-                                          if learned_line and plain_value else None),
+        "fp32_previous_correction": prev_line,
+        "net_ms_per_step": tm["net_ms"] / args.steps,
         "sweeps_per_step": sweeps / args.steps,
         "sweeps_per_s": tm["sweeps32"] / (tm["sor32_ms"] * 1e-3) if tm["sor32_ms"] else None,
         "cells_per_s": value * ncell,
@@ -527,6 +583,8 @@ def main():
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu and "cpu" in arms:
         cpu = cpu_sample(pkg, cs, sum(plain_sweeps) / len(plain_sweeps), threads)
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if net is not None:
+        net.close()
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
         "ib3d_net_dataset_reserve": (C.c_int, [_VP, C.c_int, C.c_int64]),
         "ib3d_net_dataset_size": (C.c_int64, [_VP]),
         "ib3d_net_capture": (C.c_int, [_VP, _VP, C.c_int, C.c_uint64]),
+        "ib3d_net_set_coarsening": (C.c_int, [_VP, C.c_int]),
         "ib3d_net_train": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_uint64, _D]),
         "ib3d_enable_history": (C.c_int, [_VP]),
         "ib3d_attach_net": (C.c_int, [_VP, _VP]),
@@ -451,6 +452,10 @@ class Net:
 
     def reserve(self, patch: int, capacity: int):
         self._check(self.L.ib3d_net_dataset_reserve(self._h, patch, capacity), "ib3d_net_dataset_reserve")
+
+    def set_coarsening(self, f: int):
+        """1: full resolution; 2 (default): 2x2x2 cells per voxel."""
+        self._check(self.L.ib3d_net_set_coarsening(self._h, f), "ib3d_net_set_coarsening")
 
     def dataset_size(self) -> int:
         return int(self.L.ib3d_net_dataset_size(self._h))

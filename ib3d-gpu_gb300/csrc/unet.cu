@@ -65,6 +65,7 @@ struct ib3d_net {
   bf16 *wf = nullptr, *wt = nullptr;   // BF16 copies: forward [N][27][K], transposed [K][27][N]
   int step = 0;
   Buffers buf;
+  int coarsen = 2;     // fine cells per coarse voxel edge (1: full resolution)
   // training set
   int S = 0;
   long long cap = 0, count = 0;
@@ -258,25 +259,54 @@ __global__ void __launch_bounds__(kBlock) k_hist_residual(Dims d, Grid1D g, cons
   r[tid] = out;
 }
 
-// Full-domain input volume (1 x D x H x W with the interior at the origin, padded
-// with zeros to multiples of 4).
-__global__ void k_pack_domain(Dims d, Vol v, const double* __restrict__ h1, const double* __restrict__ h2,
+// Inputs of one coarse voxel: the average of cell_inputs over the f^3 fine cells it
+// covers that lie in the domain (x0..x0+f-1 etc., 1-based interior cells from 2);
+// non-fluid cells count as zero inputs.
+__device__ __forceinline__ void coarse_inputs(const Dims& d, const unsigned char* cell, int f, int i0, int j0,
+                                              int k0, const double* h1, const double* h2, const double* bdt,
+                                              const float* r, Norm nm, float in[kInputs]) {
+  float acc[kInputs] = {};
+  int n = 0;
+  for (int dz = 0; dz < f; ++dz)
+    for (int dy = 0; dy < f; ++dy)
+      for (int dx = 0; dx < f; ++dx) {
+        const int i = i0 + dx, j = j0 + dy, k = k0 + dz;
+        if (i > d.nx + 1 || j > d.ny + 1 || k > d.nz + 1) continue;
+        ++n;
+        const long long o = d.at(i, j, k);
+        if (cell[o] != 0) continue;
+        float c[kInputs];
+        cell_inputs(o, h1, h2, bdt, r, nm, c);
+#pragma unroll
+        for (int q = 0; q < kInputs; ++q) acc[q] += c[q];
+      }
+#pragma unroll
+  for (int q = 0; q < kInputs; ++q) in[q] = n ? acc[q] / (float)n : 0.f;
+}
+
+// Full-domain input volume at coarsening f: voxel (x,y,z) covers fine cells
+// 2+f*x .. 2+f*x+f-1 (and likewise in y, z); 1 x D x H x W with D, H, W the coarse
+// extents rounded up to multiples of 4, zero outside the domain.
+__global__ void k_pack_domain(Dims d, Vol v, int f, const unsigned char* __restrict__ cell,
+                              const double* __restrict__ h1, const double* __restrict__ h2,
                               const double* __restrict__ bdt, const float* __restrict__ r, Norm nm,
                               bf16* __restrict__ in0) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= v.voxels()) return;
   const int x = (int)(m % v.W), y = (int)((m / v.W) % v.H), z = (int)(m / ((long long)v.W * v.H));
   float in[kInputs] = {};
-  if (x < d.nx && y < d.ny && z < d.nz) cell_inputs(d.at(x + 2, y + 2, z + 2), h1, h2, bdt, r, nm, in);
+  if (f * x < d.nx && f * y < d.ny && f * z < d.nz)
+    coarse_inputs(d, cell, f, 2 + f * x, 2 + f * y, 2 + f * z, h1, h2, bdt, r, nm, in);
   bf16* dst = in0 + m * 16;
 #pragma unroll
   for (int c = 0; c < kInputs; ++c) dst[c] = __float2bfloat16(in[c]);
 }
 
-// pc = (p^{n-1} - p^{n-2}) + s1 * out on fluid cells, 0 elsewhere.
-__global__ void k_unpack_domain(Dims d, Vol v, const float* __restrict__ out, const unsigned char* __restrict__ cell,
-                                const double* __restrict__ h1, const double* __restrict__ h2, double s1,
-                                double* __restrict__ pc) {
+// pc = (p^{n-1} - p^{n-2}) + s1 * out(coarse voxel of the cell) on fluid cells, 0
+// elsewhere (the coarse prediction taken back piecewise constant).
+__global__ void k_unpack_domain(Dims d, Vol v, int f, const float* __restrict__ out,
+                                const unsigned char* __restrict__ cell, const double* __restrict__ h1,
+                                const double* __restrict__ h2, double s1, double* __restrict__ pc) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (unsigned)d.n3) return;
   const int i = (int)(tid % (unsigned)d.NX2);
@@ -284,12 +314,15 @@ __global__ void k_unpack_domain(Dims d, Vol v, const float* __restrict__ out, co
   const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
   double val = 0.0;
   if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0)
-    val = (h1[tid] - h2[tid]) + s1 * (double)out[((long long)(k - 1) * v.H + (j - 1)) * v.W + (i - 1)];
+    val = (h1[tid] - h2[tid]) +
+          s1 * (double)out[((long long)((k - 1) / f) * v.H + (j - 1) / f) * v.W + (i - 1) / f];
   pc[tid] = val;
 }
 
-// One training patch: S^3 cells from origin (i0,j0,k0) (1-based interior cells).
-__global__ void k_capture(Dims d, int S, int i0, int j0, int k0, const double* __restrict__ h1,
+// One training patch of S^3 coarse voxels at coarsening f, covering the fine cells
+// from (i0,j0,k0) (1-based interior cells): the averaged inputs and the averaged
+// change of the correction over the fluid cells (0 where a voxel has none).
+__global__ void k_capture(Dims d, int S, int f, int i0, int j0, int k0, const double* __restrict__ h1,
                           const double* __restrict__ h2, const double* __restrict__ bdt,
                           const float* __restrict__ r, const double* __restrict__ pc,
                           const unsigned char* __restrict__ cell, Norm nm, bf16* __restrict__ din,
@@ -297,13 +330,22 @@ __global__ void k_capture(Dims d, int S, int i0, int j0, int k0, const double* _
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= (long long)S * S * S) return;
   const int x = (int)(m % S), y = (int)((m / S) % S), z = (int)(m / ((long long)S * S));
-  const long long o = d.at(i0 + x, j0 + y, k0 + z);
+  const int ci = i0 + f * x, cj = j0 + f * y, ck = k0 + f * z;
   float in[kInputs];
-  cell_inputs(o, h1, h2, bdt, r, nm, in);
+  coarse_inputs(d, cell, f, ci, cj, ck, h1, h2, bdt, r, nm, in);
 #pragma unroll
   for (int c = 0; c < kInputs; ++c) din[m * kInputs + c] = __float2bfloat16(in[c]);
-  // target: the change of the correction (0 where the solve holds pc at 0)
-  dt[m] = cell[o] == 0 ? (float)((pc[o] - (h1[o] - h2[o])) / nm.s1) : 0.f;
+  double t = 0.0;
+  int n = 0;
+  for (int dz = 0; dz < f; ++dz)
+    for (int dy = 0; dy < f; ++dy)
+      for (int dx = 0; dx < f; ++dx) {
+        const long long o = d.at(ci + dx, cj + dy, ck + dz);
+        if (cell[o] != 0) continue;
+        t += (pc[o] - (h1[o] - h2[o])) / nm.s1;
+        ++n;
+      }
+  dt[m] = n ? (float)(t / n) : 0.f;
 }
 
 // Gathers a batch of patches into the 16-channel input and the target.
@@ -359,16 +401,19 @@ int net_predict_pc(ib3d_ctx* c) {
   if (!n || c->hist_valid < 2) return 1;
   Norm nm;
   if (norm_for(n, c, &nm) != IB3D_OK) return 1;
-  const Vol v{1, (c->d.nz + 3) / 4 * 4, (c->d.ny + 3) / 4 * 4, (c->d.nx + 3) / 4 * 4};
+  const int f = n->coarsen;
+  const int cz = (c->d.nz + f - 1) / f, cy = (c->d.ny + f - 1) / f, cx = (c->d.nx + f - 1) / f;
+  const Vol v{1, (cz + 3) / 4 * 4, (cy + 3) / 4 * 4, (cx + 3) / 4 * 4};
   cudaStream_t saved = n->st;
   n->st = c->st;
   int rc = ensure_buffers(n, v, false);
   if (rc) { n->st = saved; return rc; }
-  k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, c->hist[0], c->hist[1], c->bdt,
-                                                                         c->r_hist, nm, n->buf.in0);
+  k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, f, c->cell, c->hist[0],
+                                                                         c->hist[1], c->bdt, c->r_hist, nm,
+                                                                         n->buf.in0);
   forward(n);
-  k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, n->buf.out, c->cell, c->hist[0],
-                                                                        c->hist[1], nm.s1, c->pc);
+  k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, f, n->buf.out, c->cell,
+                                                                        c->hist[0], c->hist[1], nm.s1, c->pc);
   n->st = saved;
   c->launches += 18;
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
@@ -497,23 +542,32 @@ int ib3d_net_dataset_reserve(ib3d_net* n, int S, int64_t capacity) {
 
 int64_t ib3d_net_dataset_size(const ib3d_net* n) { return n ? n->count : 0; }
 
+// Coarsening of capture and inference: 1 (full resolution) or 2 (the default:
+// 2x2x2 cells per voxel). Clears the training set, whose patches used the old one.
+int ib3d_net_set_coarsening(ib3d_net* n, int f) {
+  if (!n || (f != 1 && f != 2)) return IB3D_ERR_ARG;
+  n->coarsen = f;
+  n->count = 0;
+  return IB3D_OK;
+}
+
 // Adds up to npatches random S^3 patches of the context's last step (inputs from
 // the two previous pressures and this step's b/dt, target this step's pc).
 int ib3d_net_capture(ib3d_net* n, ib3d_ctx* c, int npatches, uint64_t seed) {
   if (!n || !c || npatches < 1 || !n->ds_in) return IB3D_ERR_ARG;
   if (c->hist_valid < 2) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: fewer than two previous pressures");
-  const int S = n->S;
-  if (S > c->d.nx || S > c->d.ny || S > c->d.nz) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: patch larger than grid");
+  const int S = n->S, f = n->coarsen, F = S * f;   // F fine cells per patch edge
+  if (F > c->d.nx || F > c->d.ny || F > c->d.nz) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: patch larger than grid");
   Norm nm;
   if (norm_for(n, c, &nm) != IB3D_OK) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: zero normalisation");
   std::mt19937_64 rng(seed);
   const size_t per = (size_t)S * S * S;
   for (int q = 0; q < npatches && n->count < n->cap; ++q) {
-    const int i0 = 2 + (int)(rng() % (uint64_t)(c->d.nx - S + 1));
-    const int j0 = 2 + (int)(rng() % (uint64_t)(c->d.ny - S + 1));
-    const int k0 = 2 + (int)(rng() % (uint64_t)(c->d.nz - S + 1));
-    k_capture<<<(unsigned)((per + 255) / 256), 256, 0, c->st>>>(c->d, S, i0, j0, k0, c->hist[0], c->hist[1], c->bdt,
-                                                                c->r_hist, c->pc, c->cell, nm,
+    const int i0 = 2 + (int)(rng() % (uint64_t)(c->d.nx - F + 1));
+    const int j0 = 2 + (int)(rng() % (uint64_t)(c->d.ny - F + 1));
+    const int k0 = 2 + (int)(rng() % (uint64_t)(c->d.nz - F + 1));
+    k_capture<<<(unsigned)((per + 255) / 256), 256, 0, c->st>>>(c->d, S, f, i0, j0, k0, c->hist[0], c->hist[1],
+                                                                c->bdt, c->r_hist, c->pc, c->cell, nm,
                                                                 n->ds_in + n->count * per * kInputs,
                                                                 n->ds_t + n->count * per);
     n->count++;

@@ -329,6 +329,17 @@ def sphere_case(name: str, n: tuple[int, int, int], h: float, core: float, re: f
                 stretch)
 
 
+def body_box(cs: Case, centre=(0.0, 0.0, 0.0), margin_cells: int = 4) -> tuple:
+    """Search box of a body of cs's radius centred at `centre` (the cells within
+    radius + margin_cells core cells of it), for re-tagging a moving body."""
+    h = float(np.min(np.diff(cs.x)))
+    m = cs.radius + margin_cells * h
+    box = []
+    for a, ax in enumerate((cs.x, cs.y, cs.z)):
+        box += list(search_box(ax, centre[a] - m, centre[a] + m))
+    return tuple(box)
+
+
 def case(name: str) -> Case:
     """The named workloads.
 

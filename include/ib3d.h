@@ -273,7 +273,8 @@ int ib3d_read_result_text(ib3d_ctx* ctx, const char* path, double* totime, int64
 
 /* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A 3-level 3-D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
- * activations, FP32 accumulation) predicts the change of the pressure correction
+ * activations, FP32 accumulation), applied to the domain coarsened 2x2x2 (see
+ * ib3d_net_set_coarsening), predicts the change of the pressure correction
  * from one step to the next, pc^n - pc^{n-1}, from four inputs per cell: the
  * previous correction (p^{n-1} - p^{n-2}), b/dt, p^{n-1}, and the FP64 residual of
  * the previous correction against this step's b/dt divided by the diagonal of A.
@@ -300,6 +301,13 @@ int ib3d_net_loss_grad(ib3d_net* net, int B, int S, const float* x, const float*
 int ib3d_net_dataset_reserve(ib3d_net* net, int S, int64_t capacity);
 int64_t ib3d_net_dataset_size(const ib3d_net* net);
 int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
+/* The network sees the domain coarsened by f = 1 or 2 (default 2): each voxel holds
+ * the average of the f^3 cells it covers, and the prediction is taken back to every
+ * cell of its voxel -- a learned coarse-grid correction of the smooth error that
+ * red-black SOR removes slowest, at 1/f^3 of the inference cost. Capture (S^3
+ * voxels = (fS)^3 cells per patch) and inference use the same f; changing it
+ * clears the training set. */
+int ib3d_net_set_coarsening(ib3d_net* net, int f);
 int ib3d_net_train(ib3d_net* net, int steps, int batch, double lr, uint64_t seed, double* last_loss);
 /* Keeps the two previous pressures and the previous correction's residual in ctx
  * (needed by capture and by the learned warm start); ib3d_attach_net calls it. */

@@ -3,6 +3,8 @@ kernels against a float64 PyTorch restatement of the same network on the CPU, an
 a short capture / train / solve cycle on a small case."""
 from __future__ import annotations
 
+import pathlib
+
 import numpy as np
 import pytest
 
@@ -126,7 +128,7 @@ def test_capture_train_and_learned_warm_start(ib3d, grids):
     src = ib3d.setup_case(cs, warm_start=ib3d.WARM_PREV, **common)
     src.enable_history()
     net = ib3d.Net(seed=0)
-    net.reserve(32, 256)
+    net.reserve(16, 256)         # 16^3 voxels of 2x2x2 cells: 32^3 cells of the 64x48x48 grid
     for step in range(1, 9):
         src.step(step == 1)
         if step >= 3:
@@ -152,4 +154,32 @@ def test_capture_train_and_learned_warm_start(ib3d, grids):
     assert abs((cl[0] + cl[1]) - (c64[0] + c64[1])) <= 1e-4 * abs(c64[0] + c64[1])
     for s in (src, ref, lrn):
         s.close()
+    net.close()
+
+
+WEIGHTS = pathlib.Path(__file__).resolve().parent.parent / "ib3d-gpu_gb300" / "weights" / "unet_sphere256.f32"
+
+
+def test_trained_network_saves_sweeps(ib3d, grids):
+    """What the trained network gains: on a held-out Reynolds number (275; trained
+    at 200/250/300/350) of the 256x192x192 sphere, the learned warm start needs
+    fewer SOR sweeps than the previous-correction warm start over steps 3-8 (the
+    network acts from step 3), both stopping at the same FP64 residual 1e-6 (pass
+    lengths adaptive so that the counts resolve small differences); drag and lift
+    agree within 1e-4."""
+    import dataclasses
+    import importlib
+    learned = importlib.import_module("ib3d_gpu_gb300.learned")
+    if not WEIGHTS.exists():
+        pytest.skip("no trained weights in the package")
+    net = ib3d.Net(seed=0)
+    net.set_params(np.fromfile(WEIGHTS, dtype="<f4"))
+    cs = dataclasses.replace(grids.case("sphere256"), omega=1.99, eps=1e-6)
+    ev = learned.evaluate(net, cs, 275.0, 8, inner_schedule=1)
+    prev, lrn = ev["prev"], ev["learned"]
+    saved = 1.0 - sum(lrn["sweeps"][2:]) / sum(prev["sweeps"][2:])
+    print(f"sweeps previous-correction {prev['sweeps']}, learned {lrn['sweeps']}: {100 * saved:.1f} % saved")
+    assert saved > 0.0
+    c0, c1 = np.array(prev["coef"][-1]), np.array(lrn["coef"][-1])
+    assert abs((c1[0] + c1[1]) - (c0[0] + c0[1])) <= 1e-4 * abs(c0[0] + c0[1])
     net.close()
