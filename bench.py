@@ -101,7 +101,7 @@ def load_net(pkg, path=WEIGHTS):
     return net
 
 
-def train_net(pkg, cs, out: str, seconds: float) -> dict:
+def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2) -> dict:
     """Generates snapshots (4 perturbed runs at Re 200/250/300/350, 24 steps, 8 random
     patches of 64^3 coarse voxels = 128^3 cells per step from step 3), trains with Adam
     for `seconds` (batch 8, lr 1e-3 then 2e-4 for the last 30 %), writes the FP32
@@ -111,7 +111,8 @@ def train_net(pkg, cs, out: str, seconds: float) -> dict:
     import numpy as np
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
     net = pkg.Net(seed=0)
-    net.reserve(64, 4 * 24 * 8)
+    net.set_coarsening(coarsen)
+    net.reserve(128 // coarsen, 4 * 24 * 8)     # patches of 128^3 cells
     gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 8)
     fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
     before = fit()
@@ -418,6 +419,7 @@ def main():
                     help="instead of the benchmark: generate snapshots, train the warm-start U-Net and write "
                          "its weights to this file")
     ap.add_argument("--train-seconds", type=float, default=300.0)
+    ap.add_argument("--coarsen", type=int, default=2, help="coarsening of the network trained by --train-net")
     ap.add_argument("--moving", action="store_true",
                     help="instead of the step benchmark: the transversely oscillating sphere "
                          "(y = 0.2 sin(2 pi 0.2 t), search every step) on --case (default sphere384), "
@@ -435,8 +437,8 @@ def main():
         FAST[k.strip()] = float(v) if "." in v or "e" in v else int(v)
     if args.train_net:
         if dist.rank == 0:
-            print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds)),
-                  flush=True)
+            print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds,
+                                       args.coarsen)), flush=True)
         dist.close()
         return
     if args.moving:

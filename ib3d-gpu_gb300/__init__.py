@@ -454,7 +454,7 @@ class Net:
         self._check(self.L.ib3d_net_dataset_reserve(self._h, patch, capacity), "ib3d_net_dataset_reserve")
 
     def set_coarsening(self, f: int):
-        """1: full resolution; 2 (default): 2x2x2 cells per voxel."""
+        """1: full resolution; 2 (default): 2x2x2 cells per voxel; 4: 4x4x4."""
         self._check(self.L.ib3d_net_set_coarsening(self._h, f), "ib3d_net_set_coarsening")
 
     def dataset_size(self) -> int:

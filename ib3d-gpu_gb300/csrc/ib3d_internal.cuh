@@ -218,7 +218,7 @@ int run_stress(ib3d_ctx* c, int first, double coef[4]);
 // unet.cu: pc = the attached network's prediction; nonzero when not available yet
 int run_move_body(ib3d_ctx* c, double dx, double dy, double dz);
 int net_predict_pc(ib3d_ctx* c);
-// unet.cu: r_hist = ((b/dt) - A pc) / diag(A) for the current pc
+// k_fast.cu: r_hist = ((b/dt) - A pc) / diag(A) for the current pc
 void net_hist_residual(ib3d_ctx* c);
 
 // error helper: records the message and returns IB3D_ERR_CUDA

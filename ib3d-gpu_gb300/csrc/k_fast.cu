@@ -93,7 +93,44 @@ __global__ void __launch_bounds__(kBlock) k_residual_fast(Dims d, Grid1D g, cons
   finish_block(ctl, &ctl->res, 0, sweep, eps, max_sweeps);
 }
 
+// r = ((b/dt) - A pc) / diag(A) at the fluid cells (the FP64 residual of the defect
+// correction, scaled as one Jacobi update and rounded to FP32), 0 elsewhere: the
+// previous correction's residual against this step's right-hand side, taken before
+// the guess is replaced; an input of the learned warm start (unet.cu). Dividing by
+// the diagonal takes out the local grid spacing (A ~ 1/h^2), so the input means the
+// same on the fine core and the stretched far field.
+__global__ void __launch_bounds__(kBlock) k_hist_residual(Dims d, Grid1D g, const double* __restrict__ bdt,
+                                                          const double* __restrict__ pc,
+                                                          const unsigned char* __restrict__ cell,
+                                                          float* __restrict__ r) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)d.n3) return;
+  const int i = (int)(tid % (unsigned)d.NX2);
+  const unsigned t = tid / (unsigned)d.NX2;
+  const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
+  float out = 0.f;
+  if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0) {
+    // padded index (i, j, k) 0-based is the 1-based cell (i+1, j+1, k+1)
+    const long long idx = tid, sy = d.NX2, sz = (long long)d.NX2 * d.NY2;
+    const double diag = g.acx[1][i] + g.acy[1][j] + g.acz[1][k];
+    double s = g.acx[0][i] * pc[idx - 1];
+    s = fma(g.acx[2][i], pc[idx + 1], s);
+    s = fma(g.acy[0][j], pc[idx - sy], s);
+    s = fma(g.acy[2][j], pc[idx + sy], s);
+    s = fma(g.acz[0][k], pc[idx - sz], s);
+    s = fma(g.acz[2][k], pc[idx + sz], s);
+    s = fma(diag, pc[idx], s);
+    out = (float)(bdt[idx] - s) / (float)diag;
+  }
+  r[tid] = out;
+}
+
 }  // namespace
+
+void net_hist_residual(ib3d_ctx* c) {
+  k_hist_residual<<<nblk(c->d.n3), kBlock, 0, c->st>>>(c->d, c->g, c->bdt, c->pc, c->cell, c->r_hist);
+  c->launches += 1;
+}
 
 void launch_divergence_fast(ib3d_ctx* c, bool zero_pc) {
   PhaseScope ps(c, PH_DIVERGENCE);

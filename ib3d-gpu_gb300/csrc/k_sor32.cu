@@ -56,20 +56,24 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
   }
 }
 
-// One colour pass. Block (32, 8): a warp covers 32 float4 groups of one row (j, k),
-// so the row's colour phase is uniform across the warp; grid (ceil(nq/32),
-// ceil(ny/8), ceil(nz/kPlanes)) maps the rest without integer division. A thread
+// One colour pass. Block (32, kRows): a warp covers 32 float4 groups of one row
+// (j, k), so the row's colour phase is uniform across the warp; grid (ceil(nq/32),
+// ceil(ny/kRows), ceil(nz/kPlanes)) maps the rest without integer division. A thread
 // updates its four cells in kPlanes consecutive planes, carrying the other colour's
 // centre and upper plane over to the next plane instead of loading them again.
 constexpr int kPlanes = 2;
+constexpr int kRows = 4;
 
 template <int COLOR>
-__global__ void __launch_bounds__(256) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
+__global__ void __launch_bounds__(32 * kRows) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
                                                 float* __restrict__ e_own, const float* __restrict__ e_oth,
                                                 int Lp, float omega, float om1) {
+  // launched with programmatic dependent launch: the blocks may start while the
+  // previous pass drains; wait for it (and its writes) before touching memory
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nq = ((d.nx >> 1) + 3) >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y + 2;
+  const int j = blockIdx.y * kRows + threadIdx.y + 2;
   const int k0 = blockIdx.z * kPlanes + 2;
   if (q >= nq || j > d.ny + 1) return;
   const long long plane = (long long)(d.ny + 2) * Lp;
@@ -108,6 +112,8 @@ __global__ void __launch_bounds__(256) k_sor32p(Dims d, Grid1D g, const float* _
     ob = ox;
     ox = ot;
   }
+  // the next pass may launch now; its griddepcontrol.wait still waits for this grid
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // pc += e at every interior cell, reading e from its colour's packed array, then
@@ -132,12 +138,27 @@ __global__ void k_accumulate_packed(Dims d, double* __restrict__ pc, float* __re
 void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   const Dims& d = c->d;
   const int nq = ((d.nx >> 1) + 3) >> 2;
-  const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)((d.nz + kPlanes - 1) / kPlanes)),
-      block(32, 8);
+  const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((d.ny + kRows - 1) / kRows),
+                  (unsigned)((d.nz + kPlanes - 1) / kPlanes)),
+      block(32, kRows);
+  // programmatic dependent launch: the colour passes run back to back, and the launch
+  // and block start-up of one overlap the tail of the previous one
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (color == 0)
-    k_sor32p<0><<<grid, block, 0, c->st>>>(d, c->g, c->rp[0], c->ep[0], c->ep[1], c->packed_lp, omega, om1);
+    cudaLaunchKernelEx(&cfg, k_sor32p<0>, d, c->g, (const float*)c->rp[0], c->ep[0], (const float*)c->ep[1],
+                       c->packed_lp, omega, om1);
   else
-    k_sor32p<1><<<grid, block, 0, c->st>>>(d, c->g, c->rp[1], c->ep[1], c->ep[0], c->packed_lp, omega, om1);
+    cudaLaunchKernelEx(&cfg, k_sor32p<1>, d, c->g, (const float*)c->rp[1], c->ep[1], (const float*)c->ep[0],
+                       c->packed_lp, omega, om1);
 }
 
 void launch_accumulate_packed(ib3d_ctx* c) {

@@ -72,7 +72,7 @@ struct ib3d_net {
   bf16* ds_in = nullptr;   // [patch][S^3][4]
   float* ds_t = nullptr;   // [patch][S^3]
   double* d_loss = nullptr;
-  double* d_red = nullptr; // reductions for normalisation
+  double* d_red = nullptr; // normalisation sums [5] and per-block partials (from [8])
 };
 
 namespace {
@@ -195,13 +195,18 @@ void cast_weights(ib3d_net* n) {
 // ------------------------------------------------------------- data kernels
 
 // RMS inputs over fluid cells: sums of (h1-h2)^2, (b/dt)^2, h1^2, r^2 and the
-// fluid count.
-__global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, const double* __restrict__ h1,
-                            const double* __restrict__ h2, const double* __restrict__ bdt,
-                            const float* __restrict__ r, double* sums) {
-  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+// fluid count. kNormBlocks blocks stride over the cells and write one partial sum
+// per block; k_norm_final adds the partials in block order, so the result does not
+// depend on scheduling (and needs no atomics on five contended addresses).
+constexpr int kNormBlocks = 1216;
+__global__ void __launch_bounds__(256) k_norm_sums(Dims d, const unsigned char* __restrict__ cell,
+                                                   const double* __restrict__ h1, const double* __restrict__ h2,
+                                                   const double* __restrict__ bdt, const float* __restrict__ r,
+                                                   double* __restrict__ partial) {
+  __shared__ double sm[8][5];
   double s[5] = {0, 0, 0, 0, 0};
-  if (tid < (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz) {
+  const unsigned n = (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz;
+  for (unsigned tid = blockIdx.x * blockDim.x + threadIdx.x; tid < n; tid += gridDim.x * blockDim.x) {
     const int i = (int)(tid % (unsigned)d.nx) + 2;
     const unsigned t = tid / (unsigned)d.nx;
     const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
@@ -209,54 +214,42 @@ __global__ void k_norm_sums(Dims d, const unsigned char* __restrict__ cell, cons
     if (cell[o] == 0) {
       const double dp = h1[o] - h2[o];
       const double rr = (double)r[o];
-      s[0] = dp * dp; s[1] = bdt[o] * bdt[o]; s[2] = h1[o] * h1[o]; s[3] = rr * rr; s[4] = 1.0;
+      s[0] += dp * dp; s[1] += bdt[o] * bdt[o]; s[2] += h1[o] * h1[o]; s[3] += rr * rr; s[4] += 1.0;
     }
   }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int q = 0; q < 5; ++q) {
     double x = s[q];
     for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-    if ((threadIdx.x & 31) == 0 && x != 0.0) atomicAdd(&sums[q], x);
+    if (lane == 0) sm[wid][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double x = 0.0;
+    for (int w = 0; w < 8; ++w) x += sm[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * 5 + threadIdx.x] = x;
   }
 }
 
+__global__ void k_norm_final(const double* __restrict__ partial, int nblocks, double* __restrict__ sums) {
+  if (threadIdx.x >= 5) return;
+  double x = 0.0;
+  for (int b = 0; b < nblocks; ++b) x += partial[(size_t)b * 5 + threadIdx.x];
+  sums[threadIdx.x] = x;
+}
+
 struct Norm {
-  double s1, s2, s3, s4;
+  double s1, s2, s3, s4;   // RMS of each input over the fluid cells
+  double r1, r2, r3, r4;   // their reciprocals (inputs are scaled by products)
 };
 
 // Input channels of one cell (see the file header); channels kInputs..15 are zero.
 __device__ __forceinline__ void cell_inputs(long long o, const double* h1, const double* h2, const double* bdt,
                                             const float* r, Norm nm, float in[kInputs]) {
-  in[0] = (float)((h1[o] - h2[o]) / nm.s1);
-  in[1] = (float)(bdt[o] / nm.s2);
-  in[2] = (float)(h1[o] / nm.s3);
-  in[3] = (float)((double)r[o] / nm.s4);
-}
-
-// r = ((b/dt) - A pc) / diag(A) at the fluid cells (the FP64 residual of the defect
-// correction, scaled as one Jacobi update), 0 elsewhere: the previous correction's
-// residual against this step's right-hand side, taken before the guess is replaced.
-// Dividing by the diagonal takes out the local grid spacing (A ~ 1/h^2), so the
-// input means the same on the fine core and the stretched far field.
-__global__ void __launch_bounds__(kBlock) k_hist_residual(Dims d, Grid1D g, const double* __restrict__ bdt,
-                                                          const double* __restrict__ pc,
-                                                          const unsigned char* __restrict__ cell,
-                                                          float* __restrict__ r) {
-  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= (unsigned)d.n3) return;
-  const int i = (int)(tid % (unsigned)d.NX2);
-  const unsigned t = tid / (unsigned)d.NX2;
-  const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
-  float out = 0.f;
-  if (i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz && cell[tid] == 0) {
-    // padded index (i, j, k) 0-based is the 1-based cell (i+1, j+1, k+1)
-    const long long idx = tid, sy = d.NX2, sz = (long long)d.NX2 * d.NY2;
-    const double num = bdt[idx] - g.acx[0][i] * pc[idx - 1] - g.acx[2][i] * pc[idx + 1] -
-                       g.acy[0][j] * pc[idx - sy] - g.acy[2][j] * pc[idx + sy] - g.acz[0][k] * pc[idx - sz] -
-                       g.acz[2][k] * pc[idx + sz];
-    const double diag = g.acx[1][i] + g.acy[1][j] + g.acz[1][k];
-    out = (float)((num - diag * pc[idx]) / diag);
-  }
-  r[tid] = out;
+  in[0] = (float)((h1[o] - h2[o]) * nm.r1);
+  in[1] = (float)(bdt[o] * nm.r2);
+  in[2] = (float)(h1[o] * nm.r3);
+  in[3] = r[o] * (float)nm.r4;
 }
 
 // Inputs of one coarse voxel: the average of cell_inputs over the f^3 fine cells it
@@ -342,7 +335,7 @@ __global__ void k_capture(Dims d, int S, int f, int i0, int j0, int k0, const do
       for (int dx = 0; dx < f; ++dx) {
         const long long o = d.at(ci + dx, cj + dy, ck + dz);
         if (cell[o] != 0) continue;
-        t += (pc[o] - (h1[o] - h2[o])) / nm.s1;
+        t += (pc[o] - (h1[o] - h2[o])) * nm.r1;
         ++n;
       }
   dt[m] = n ? (float)(t / n) : 0.f;
@@ -369,10 +362,9 @@ __global__ void k_set_input(long long M, const float* __restrict__ x, bf16* __re
 }
 
 int norm_for(ib3d_net* n, ib3d_ctx* c, Norm* nm) {
-  NET_CUDA(n, cudaMemsetAsync(n->d_red, 0, 5 * sizeof(double), c->st));
-  const long long ncell = (long long)c->d.nx * c->d.ny * c->d.nz;
-  k_norm_sums<<<(unsigned)((ncell + 255) / 256), 256, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt,
-                                                                   c->r_hist, n->d_red);
+  k_norm_sums<<<kNormBlocks, 256, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt, c->r_hist,
+                                               n->d_red + 8);
+  k_norm_final<<<1, 32, 0, c->st>>>(n->d_red + 8, kNormBlocks, n->d_red);
   double h[5];
   NET_CUDA(n, cudaMemcpyAsync(h, n->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
   NET_CUDA(n, cudaStreamSynchronize(c->st));
@@ -382,18 +374,16 @@ int norm_for(ib3d_net* n, ib3d_ctx* c, Norm* nm) {
   nm->s2 = std::sqrt(h[1] / h[4]);
   nm->s3 = std::sqrt(h[2] / h[4]);
   nm->s4 = std::sqrt(h[3] / h[4]);
+  nm->r1 = 1.0 / nm->s1;
+  nm->r2 = 1.0 / nm->s2;
+  nm->r3 = 1.0 / nm->s3;
+  nm->r4 = 1.0 / nm->s4;
   return IB3D_OK;
 }
 
 }  // namespace
 
 namespace ib3d {
-void net_hist_residual(ib3d_ctx* c) {
-  k_hist_residual<<<(unsigned)((c->d.n3 + kBlock - 1) / kBlock), kBlock, 0, c->st>>>(c->d, c->g, c->bdt, c->pc, c->cell,
-                                                                                    c->r_hist);
-  c->launches += 1;
-}
-
 // Called by the pressure solve: pc = network prediction (returns nonzero when the
 // history or the normalisation is not available yet; pc is then left unchanged).
 int net_predict_pc(ib3d_ctx* c) {
@@ -450,7 +440,7 @@ int ib3d_net_create(ib3d_net** out, uint64_t seed) {
   for (float** q : fb) ok = ok && cudaMalloc(q, n->nparam * sizeof(float)) == cudaSuccess;
   ok = ok && cudaMalloc(&n->wf, n->nparam * sizeof(bf16)) == cudaSuccess &&
        cudaMalloc(&n->wt, n->nparam * sizeof(bf16)) == cudaSuccess &&
-       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, 5 * sizeof(double)) == cudaSuccess;
+       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, (8 + 5 * (size_t)kNormBlocks) * sizeof(double)) == cudaSuccess;
   if (!ok) {
     ib3d_net_destroy(n);
     return IB3D_ERR_MEMORY;
@@ -542,10 +532,10 @@ int ib3d_net_dataset_reserve(ib3d_net* n, int S, int64_t capacity) {
 
 int64_t ib3d_net_dataset_size(const ib3d_net* n) { return n ? n->count : 0; }
 
-// Coarsening of capture and inference: 1 (full resolution) or 2 (the default:
-// 2x2x2 cells per voxel). Clears the training set, whose patches used the old one.
+// Coarsening of capture and inference: 1 (full resolution), 2 (the default: 2x2x2
+// cells per voxel) or 4. Clears the training set, whose patches used the old one.
 int ib3d_net_set_coarsening(ib3d_net* n, int f) {
-  if (!n || (f != 1 && f != 2)) return IB3D_ERR_ARG;
+  if (!n || (f != 1 && f != 2 && f != 4)) return IB3D_ERR_ARG;
   n->coarsen = f;
   n->count = 0;
   return IB3D_OK;

@@ -3,8 +3,9 @@
 The network is trained on snapshots the solver generates: runs of a sphere case at
 several Reynolds numbers, each started from u = 1 with a seeded 1 % random
 perturbation of the initial streamwise velocity, solved with the previous
-correction as warm start while ib3d_net_capture stores random S^3 patches of every
-step (inputs and the solved change of the correction). Training is Adam on random
+correction as warm start while ib3d_net_capture stores random patches of S^3
+voxels (each voxel the average of 2x2x2 cells) of every step: the inputs and the
+solved change of the correction. Training is Adam on random
 batches of those patches. Evaluation runs a held-out Reynolds number twice, once
 warm-started from the previous correction and once from the network, and compares
 the SOR sweeps and the drag/lift at the same FP64 residual tolerance.

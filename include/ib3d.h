@@ -301,7 +301,7 @@ int ib3d_net_loss_grad(ib3d_net* net, int B, int S, const float* x, const float*
 int ib3d_net_dataset_reserve(ib3d_net* net, int S, int64_t capacity);
 int64_t ib3d_net_dataset_size(const ib3d_net* net);
 int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
-/* The network sees the domain coarsened by f = 1 or 2 (default 2): each voxel holds
+/* The network sees the domain coarsened by f = 1, 2 or 4 (default 2): each voxel holds
  * the average of the f^3 cells it covers, and the prediction is taken back to every
  * cell of its voxel -- a learned coarse-grid correction of the smooth error that
  * red-black SOR removes slowest, at 1/f^3 of the inference cost. Capture (S^3

@@ -1,6 +1,7 @@
 """The learned warm start's U-Net: forward and backward of the library's own BF16
-kernels against a float64 PyTorch restatement of the same network on the CPU, and
-a short capture / train / solve cycle on a small case."""
+kernels against a float64 PyTorch restatement of the same network on the CPU, a
+short capture / train / solve cycle on a small case, and the sweeps the trained
+network in the package saves on a held-out run."""
 from __future__ import annotations
 
 import pathlib
