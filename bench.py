@@ -84,20 +84,30 @@ FAST = dict(precision=1, warm_start=1, criterion=1, inner_sweeps=256, omega_inne
             max_sweeps=400000)
 PLAIN = dict(precision=0, warm_start=0, criterion=1, check_every=8, max_sweeps=400000)
 SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
-# U-Net weights trained on the GPU by this library's own kernels (bench.py --train-net)
-WEIGHTS = ROOT / "ib3d-gpu_gb300" / "weights" / "unet_sphere256.f32"
+# U-Net weights trained on the GPU by this library's own kernels (bench.py --train-net);
+# networks.json names the default and each file's coarsening
+WEIGHTS_DIR = ROOT / "ib3d-gpu_gb300" / "weights"
 
 
-def load_net(pkg, path=WEIGHTS):
-    """The trained warm-start network, or None when no weights file exists."""
+def load_net(pkg, name: str = ""):
+    """The trained warm-start network (networks.json's default, or `name`), or None
+    when no weights are present."""
     import numpy as np
-    if not pathlib.Path(path).exists():
+    manifest = WEIGHTS_DIR / "networks.json"
+    if not manifest.exists():
+        return None
+    info = json.loads(manifest.read_text())
+    name = name or info["default"]
+    path = WEIGHTS_DIR / name
+    if not path.exists():
         return None
     net = pkg.Net(seed=0)
+    net.set_coarsening(int(info["networks"][name]["coarsen"]))
     w = np.fromfile(path, dtype="<f4")
     if w.size != net.nparams:
         raise SystemExit(f"{path}: {w.size} weights, the network has {net.nparams}")
     net.set_params(w)
+    net.weights = name
     return net
 
 
@@ -113,6 +123,7 @@ def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2) -> dict:
     net = pkg.Net(seed=0)
     net.set_coarsening(coarsen)
     net.reserve(128 // coarsen, 4 * 24 * 8)     # patches of 128^3 cells
+    net.coarsen = coarsen
     gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 8)
     fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
     before = fit()
@@ -419,7 +430,8 @@ def main():
                     help="instead of the benchmark: generate snapshots, train the warm-start U-Net and write "
                          "its weights to this file")
     ap.add_argument("--train-seconds", type=float, default=300.0)
-    ap.add_argument("--coarsen", type=int, default=2, help="coarsening of the network trained by --train-net")
+    ap.add_argument("--coarsen", type=int, default=4, help="coarsening of the network trained by --train-net")
+    ap.add_argument("--weights", default="", help="weights file in ib3d-gpu_gb300/weights (default: networks.json's)")
     ap.add_argument("--moving", action="store_true",
                     help="instead of the step benchmark: the transversely oscillating sphere "
                          "(y = 0.2 sin(2 pi 0.2 t), search every step) on --case (default sphere384), "
@@ -501,7 +513,7 @@ def main():
     arms = set(args.arms.split(","))
     # Headline: FP32 sweeps in FP64 defect correction with the learned warm start (the
     # trained network in the package); without weights, the previous-correction warm start.
-    net = load_net(pkg) if "learned" in arms else None
+    net = load_net(pkg, args.weights) if "learned" in arms else None
     head_mode = dict(FAST, warm_start=pkg.WARM_LEARNED) if net is not None else FAST
     clocks = Clocks(dist.local)
     fast = run_arm(pkg, cs, head_mode, warmup, args.steps, dist, timers=True, clocks=clocks, net=net)
@@ -552,8 +564,8 @@ def main():
                                f"Re {cs.re:g}, dt {cs.dt:g}, red-black SOR omega {cs.omega:g} to FP64 residual "
                                f"L-inf <= {cs.eps:g}",
                    "mode": ("FP32 red-black sweeps inside FP64 defect correction, inner relaxation 1.994, "
-                            + ("learned warm start (BF16 U-Net on the 2x2x2-coarsened domain, weights "
-                               f"{WEIGHTS.relative_to(ROOT)})" if net is not None
+                            + (f"learned warm start (BF16 U-Net on the {net.coarsen}x{net.coarsen}x{net.coarsen}"
+                               f"-coarsened domain, weights ib3d-gpu_gb300/weights/{net.weights})" if net is not None
                                else "warm start from the previous step's correction")),
                    "inner_sweeps": FAST["inner_sweeps"],
                    "l2": "inputs larger than L2: each step reads/writes 7 FP64 fields of 77.7 MB",

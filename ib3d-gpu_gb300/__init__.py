@@ -409,6 +409,7 @@ class Net:
         if rc != OK:
             raise IB3DError(rc, "ib3d_net_create failed")
         self.nparams = int(self.L.ib3d_net_num_params(self._h))
+        self.coarsen = 2
 
     def _check(self, rc: int, what: str):
         if rc != OK:
@@ -456,6 +457,7 @@ class Net:
     def set_coarsening(self, f: int):
         """1: full resolution; 2 (default): 2x2x2 cells per voxel; 4: 4x4x4."""
         self._check(self.L.ib3d_net_set_coarsening(self._h, f), "ib3d_net_set_coarsening")
+        self.coarsen = f
 
     def dataset_size(self) -> int:
         return int(self.L.ib3d_net_dataset_size(self._h))

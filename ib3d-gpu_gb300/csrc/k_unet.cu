@@ -6,13 +6,16 @@
 // offset co), which is how the U-Net's skip concatenations are stored. Channel
 // counts are multiples of 16.
 //
-// 3x3x3 convolutions (zero padding) are implicit GEMMs on the BF16 tensor cores
-// (mma.sync m16n8k16, FP32 accumulators): rows are voxels, columns are output
-// channels, and the reduction runs over 27 taps x input channels, gathering each
-// A fragment straight from the channels-last activations (two consecutive
-// channels per 32-bit load). The same kernel computes the input gradient with
-// mirrored taps and transposed weights. Weight gradients are reduced on the CUDA
-// cores in FP32.
+// 3x3x3 convolutions (zero padding) are implicit GEMMs on the fifth-generation
+// tensor cores (tcgen05.mma kind::f16, BF16 operands from shared memory, FP32
+// accumulator in tensor memory): rows are 128 voxels of a block, columns the
+// output channels, and the reduction runs over 27 taps x input channels in steps of
+// 16 channels. The threads gather each step's A tile (the 128 voxels' neighbours,
+// 16 channels each) and B tile (the weights) into a double-buffered shared-memory
+// stage in the canonical no-swizzle K-major layout, one thread issues the MMA, and
+// a tcgen05.commit to the stage's mbarrier frees it for the step after next. The
+// same kernel computes the input gradient with mirrored taps and transposed
+// weights. Weight gradients are reduced on the CUDA cores in FP32.
 #include <cuda_bf16.h>
 
 #include "ib3d_internal.cuh"
@@ -23,15 +26,28 @@ namespace unet {
 
 namespace {
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of 8 rows x 16
+// bytes; lbo = byte distance between core matrices along K, sbo = along M/N.
+__device__ __forceinline__ unsigned long long smem_desc(const void* p, unsigned lbo, unsigned sbo) {
+  unsigned long long d = (unsigned long long)((smem_addr(p) & 0x3FFFF) >> 4);
+  d |= (unsigned long long)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (unsigned long long)((sbo >> 4) & 0x3FFF) << 32;
+  d |= 1ull << 46;   // descriptor version; base offset 0, no swizzle
+  return d;
 }
 
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+// Bounded wait on an mbarrier phase (true when it completed).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase, int limit) {
+  for (int it = 0; it < limit; ++it) {
+    unsigned ok;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(ok) : "r"(smem_addr(bar)), "r"(phase) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
 
 __device__ __forceinline__ void decode(long long m, const Vol& v, int& b, int& z, int& y, int& x) {
   x = (int)(m % v.W);
@@ -44,80 +60,119 @@ __device__ __forceinline__ void decode(long long m, const Vol& v, int& b, int& z
 
 }  // namespace
 
-// Y[v][n] = act( sum_{tap,k} X[v + sign*off(tap)][k] * Wt[n][tap][k] + bias[n] ).
-// One warp computes 32 voxels x (8*NT) channels.
-template <int NT>
+// Y[v][n] = act( sum_{tap,k} X[v + sign*off(tap)][k] * Wt[n][tap][k] + bias[n] ),
+// N output channels (a multiple of 16, at most 128). Block: 128 threads, 128
+// consecutive voxels; D in tensor memory (128 lanes x N FP32 columns). Every wait
+// is bounded and decided for the whole block: a barrier that does not complete sets
+// *err, and the kernel still waits (bounded) for its issued MMAs before it frees the
+// tensor memory.
+template <int N>
 __global__ void __launch_bounds__(128) k_conv3(Vol vol, Act X, int K, const bf16* __restrict__ Wt,
-                                               const float* __restrict__ bias, int relu, int sign, Act Y) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t4 = lane & 3;
+                                               const float* __restrict__ bias, int relu, int sign, Act Y, int* err) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 128, "tcgen05 N");
+  __shared__ __align__(128) bf16 sA[2][128 * 16];
+  __shared__ __align__(128) bf16 sB[2][N * 16];
+  __shared__ __align__(8) unsigned long long bar[3];
+  __shared__ unsigned tmem_base;
+  constexpr unsigned kCols = N <= 32 ? 32 : (N <= 64 ? 64 : 128);   // power of two >= N
+  const int t = threadIdx.x, warp = t >> 5;
   const long long M = vol.voxels();
-  const long long m0 = ((long long)blockIdx.x * 4 + warp) * 32;
-  if (m0 >= M) return;
-  int vb[4], vz[4], vy[4], vx[4];
-  bool vok[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const long long m = m0 + g + 8 * r;
-    vok[r] = m < M;
-    decode(vok[r] ? m : 0, vol, vb[r], vz[r], vy[r], vx[r]);
+  const long long m = (long long)blockIdx.x * 128 + t;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_addr(&tmem_base)), "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  float acc[2][NT][4];
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
-  for (int tap = 0; tap < 27; ++tap) {
+  if (t == 0) {
+    for (int q = 0; q < 3; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&bar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = tmem_base;
+  int vb = 0, vz = 0, vy = 0, vx = 0;
+  const bool vok = m < M;
+  if (vok) decode(m, vol, vb, vz, vy, vx);
+  // instruction descriptor: D FP32, A and B BF16, both K-major, N, M = 128
+  const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((128u >> 4) << 24);
+  const int kchunks = K / 16, steps = 27 * kchunks;
+  unsigned phase[2] = {0, 0};
+  bool ok = true;
+  for (int s = 0; s < steps; ++s) {
+    const int st = s & 1;
+    if (s >= 2) {   // the MMA that read this stage two steps ago must be done
+      ok = __syncthreads_and(mbar_wait(&bar[st], phase[st], 1 << 20)) != 0;
+      phase[st] ^= 1;
+      if (!ok) break;
+    }
+    const int tap = s / kchunks, kc = (s % kchunks) * 16;
     const int dz = sign * (tap / 9 - 1), dy = sign * ((tap / 3) % 3 - 1), dx = sign * (tap % 3 - 1);
-    const bf16* src[4];
-    bool ok[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int z = vz[r] + dz, y = vy[r] + dy, x = vx[r] + dx;
-      ok[r] = vok[r] && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W;
-      const long long sv = (((long long)vb[r] * vol.D + (ok[r] ? z : 0)) * vol.H + (ok[r] ? y : 0)) * vol.W +
-                           (ok[r] ? x : 0);
-      src[r] = X.p + sv * X.cs + X.co + 2 * t4;
+    uint4 h0 = make_uint4(0, 0, 0, 0), h1 = make_uint4(0, 0, 0, 0);
+    const int z = vz + dz, y = vy + dy, x = vx + dx;
+    if (vok && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W) {
+      const long long sv = (((long long)vb * vol.D + z) * vol.H + y) * vol.W + x;
+      const uint4* src = reinterpret_cast<const uint4*>(X.p + sv * X.cs + X.co + kc);
+      h0 = src[0];
+      h1 = src[1];
     }
-    const bf16* wbase = Wt + (size_t)tap * K + 2 * t4;
-    for (int kc = 0; kc < K; kc += 16) {
-      uint32_t a[2][4];
+    const int g = t >> 3, rr = t & 7;   // core-matrix row group and row of this thread's A row
+    char* a = reinterpret_cast<char*>(sA[st]);
+    *reinterpret_cast<uint4*>(a + (g * 2 + 0) * 128 + rr * 16) = h0;
+    *reinterpret_cast<uint4*>(a + (g * 2 + 1) * 128 + rr * 16) = h1;
+    if (t < N) {
+      const uint4* w = reinterpret_cast<const uint4*>(Wt + ((size_t)t * 27 + tap) * K + kc);
+      char* bsm = reinterpret_cast<char*>(sB[st]);
+      *reinterpret_cast<uint4*>(bsm + (g * 2 + 0) * 128 + rr * 16) = w[0];
+      *reinterpret_cast<uint4*>(bsm + (g * 2 + 1) * 128 + rr * 16) = w[1];
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // make the stage visible to the tensor core
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const unsigned long long ad = smem_desc(sA[st], 128, 256), bd = smem_desc(sB[st], 128, 256);
+      asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                   " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                   :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(s > 0 ? 1u : 0u) : "memory");
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   :: "r"(smem_addr(&bar[st])) : "memory");
+    }
+  }
+  // a commit after the last MMA arrives once every MMA of this thread is done
+  if (t == 0)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_addr(&bar[2])) : "memory");
+  const bool done = __syncthreads_and(mbar_wait(&bar[2], 0, 1 << 20)) != 0;
+  if (!ok || !done) {
+    if (t == 0) atomicExch(err, 1);
+    if (!done) mbar_wait(&bar[2], 0, 1 << 20);   // let the issued MMAs finish before freeing the columns
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const int r0 = 2 * mt, r1 = 2 * mt + 1;
-        a[mt][0] = ok[r0] ? ld_pair(src[r0] + kc) : 0u;
-        a[mt][1] = ok[r1] ? ld_pair(src[r1] + kc) : 0u;
-        a[mt][2] = ok[r0] ? ld_pair(src[r0] + kc + 8) : 0u;
-        a[mt][3] = ok[r1] ? ld_pair(src[r1] + kc + 8) : 0u;
-      }
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      unsigned r[16];
+      const unsigned addr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;   // this warp's 32 lanes
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                     "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                     "=r"(r[14]), "=r"(r[15])
+                   : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (vok) {
+        bf16* dst = Y.p + m * Y.cs + Y.co + c0;
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const bf16* wp = wbase + (size_t)(nt * 8 + g) * 27 * K + kc;
-        const uint32_t b0 = ld_pair(wp), b1 = ld_pair(wp + 8);
-        mma_bf16(acc[0][nt], a[0], b0, b1);
-        mma_bf16(acc[1][nt], a[1], b0, b1);
+        for (int q = 0; q < 16; q += 2) {
+          float v0 = __uint_as_float(r[q]), v1 = __uint_as_float(r[q + 1]);
+          if (bias) { v0 += bias[c0 + q]; v1 += bias[c0 + q + 1]; }
+          if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+          *reinterpret_cast<__nv_bfloat162*>(dst + q) = __floats2bfloat162_rn(v0, v1);
+        }
       }
     }
   }
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int r = 2 * mt + h;
-      if (!vok[r]) continue;
-      const long long m = m0 + g + 8 * r;
-      bf16* dst = Y.p + m * Y.cs + Y.co;
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const int n = nt * 8 + 2 * t4;
-        float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
-        if (bias) { v0 += bias[n]; v1 += bias[n + 1]; }
-        if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-        *reinterpret_cast<__nv_bfloat162*>(dst + n) = __floats2bfloat162_rn(v0, v1);
-      }
-    }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kCols));
 }
 
 // dW[n][tap][k] += sum_v dZ[v][n] * X[v + off(tap)][k]   (FP32, CUDA cores)
@@ -336,15 +391,15 @@ __global__ void k_cast_conv_weights(int N, int K, const float* __restrict__ w, b
 // ------------------------------------------------------------ launch helpers
 
 void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const float* bias, int relu, int sign, Act Y,
-          int N) {
+          int N, int* err) {
   const long long M = vol.voxels();
   const unsigned nb = (unsigned)((M + 127) / 128);
   switch (N) {
-    case 16: k_conv3<2><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
-    case 32: k_conv3<4><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
-    case 48: k_conv3<6><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
-    case 64: k_conv3<8><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
-    case 96: k_conv3<12><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y); break;
+    case 16: k_conv3<16><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 32: k_conv3<32><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 48: k_conv3<48><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 64: k_conv3<64><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 96: k_conv3<96><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
     default: break;
   }
 }

@@ -72,6 +72,7 @@ struct ib3d_net {
   bf16* ds_in = nullptr;   // [patch][S^3][4]
   float* ds_t = nullptr;   // [patch][S^3]
   double* d_loss = nullptr;
+  int* d_err = nullptr;    // set by a convolution whose tensor-core wait gave up
   double* d_red = nullptr; // normalisation sums [5] and per-block partials (from [8])
 };
 
@@ -80,6 +81,15 @@ namespace {
 int fail(ib3d_net* n, int code, const char* msg) {
   if (n) n->err = msg;
   return code;
+}
+
+// After a synchronisation: a convolution whose tensor-core wait gave up leaves its
+// output invalid; report it (and keep reporting it).
+int check_conv(ib3d_net* n) {
+  int h = 0;
+  if (cudaMemcpy(&h, n->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(n, IB3D_ERR_CUDA, "ib3d_net: reading the convolution status failed");
+  return h ? fail(n, IB3D_ERR_CUDA, "ib3d_net: a tensor-core wait timed out") : IB3D_OK;
 }
 #define NET_CUDA(n, expr)                                                              \
   do {                                                                                 \
@@ -139,20 +149,20 @@ const float* bias(ib3d_net* n, int l) { return n->p + n->L[l].b; }
 void forward(ib3d_net* n) {
   Buffers& b = n->buf;
   cudaStream_t st = n->st;
-  conv(st, b.v1, A(b.in0, 16), 16, wf(n, 0), bias(n, 0), 1, 1, A(b.a1, 16), 16);
-  conv(st, b.v1, A(b.a1, 16), 16, wf(n, 1), bias(n, 1), 1, 1, A(b.cat5, 48, 32), 16);   // e1
+  conv(st, b.v1, A(b.in0, 16), 16, wf(n, 0), bias(n, 0), 1, 1, A(b.a1, 16), 16, n->d_err);
+  conv(st, b.v1, A(b.a1, 16), 16, wf(n, 1), bias(n, 1), 1, 1, A(b.cat5, 48, 32), 16, n->d_err);   // e1
   pool_fwd(st, b.v2, 16, A(b.cat5, 48, 32), A(b.p1, 16));
-  conv(st, b.v2, A(b.p1, 16), 16, wf(n, 2), bias(n, 2), 1, 1, A(b.a2, 32), 32);
-  conv(st, b.v2, A(b.a2, 32), 32, wf(n, 3), bias(n, 3), 1, 1, A(b.cat4, 96, 64), 32);   // e2
+  conv(st, b.v2, A(b.p1, 16), 16, wf(n, 2), bias(n, 2), 1, 1, A(b.a2, 32), 32, n->d_err);
+  conv(st, b.v2, A(b.a2, 32), 32, wf(n, 3), bias(n, 3), 1, 1, A(b.cat4, 96, 64), 32, n->d_err);   // e2
   pool_fwd(st, b.v3, 32, A(b.cat4, 96, 64), A(b.p2, 32));
-  conv(st, b.v3, A(b.p2, 32), 32, wf(n, 4), bias(n, 4), 1, 1, A(b.a3, 64), 64);
-  conv(st, b.v3, A(b.a3, 64), 64, wf(n, 5), bias(n, 5), 1, 1, A(b.b, 64), 64);
+  conv(st, b.v3, A(b.p2, 32), 32, wf(n, 4), bias(n, 4), 1, 1, A(b.a3, 64), 64, n->d_err);
+  conv(st, b.v3, A(b.a3, 64), 64, wf(n, 5), bias(n, 5), 1, 1, A(b.b, 64), 64, n->d_err);
   up_fwd(st, b.v2, 64, A(b.b, 64), A(b.cat4, 96, 0));
-  conv(st, b.v2, A(b.cat4, 96), 96, wf(n, 6), bias(n, 6), 1, 1, A(b.a4, 32), 32);
-  conv(st, b.v2, A(b.a4, 32), 32, wf(n, 7), bias(n, 7), 1, 1, A(b.d2, 32), 32);
+  conv(st, b.v2, A(b.cat4, 96), 96, wf(n, 6), bias(n, 6), 1, 1, A(b.a4, 32), 32, n->d_err);
+  conv(st, b.v2, A(b.a4, 32), 32, wf(n, 7), bias(n, 7), 1, 1, A(b.d2, 32), 32, n->d_err);
   up_fwd(st, b.v1, 32, A(b.d2, 32), A(b.cat5, 48, 0));
-  conv(st, b.v1, A(b.cat5, 48), 48, wf(n, 8), bias(n, 8), 1, 1, A(b.a5, 16), 16);
-  conv(st, b.v1, A(b.a5, 16), 16, wf(n, 9), bias(n, 9), 1, 1, A(b.d1, 16), 16);
+  conv(st, b.v1, A(b.cat5, 48), 48, wf(n, 8), bias(n, 8), 1, 1, A(b.a5, 16), 16, n->d_err);
+  conv(st, b.v1, A(b.a5, 16), 16, wf(n, 9), bias(n, 9), 1, 1, A(b.d1, 16), 16, n->d_err);
   head_fwd(st, b.v1.voxels(), 16, A(b.d1, 16), n->p + n->head, b.out);
 }
 
@@ -164,7 +174,7 @@ void conv_bwd(ib3d_net* n, int l, const Vol& v, Act X, Act Y, Act gY, Act gX) {
   relu_bwd(n->st, M, ly.N, gY, Y);
   bias_grad(n->st, M, gY, ly.N, n->g + ly.b);
   wgrad(n->st, v, gY, ly.N, X, ly.K, n->g + ly.w);
-  if (gX.p) conv(n->st, v, gY, ly.N, wt(n, l), nullptr, 0, -1, gX, ly.K);
+  if (gX.p) conv(n->st, v, gY, ly.N, wt(n, l), nullptr, 0, -1, gX, ly.K, n->d_err);
 }
 
 void backward(ib3d_net* n) {
@@ -391,6 +401,7 @@ int net_predict_pc(ib3d_ctx* c) {
   if (!n || c->hist_valid < 2) return 1;
   Norm nm;
   if (norm_for(n, c, &nm) != IB3D_OK) return 1;
+  if (check_conv(n) != IB3D_OK) return 1;   // a failed convolution earlier: keep the previous correction
   const int f = n->coarsen;
   const int cz = (c->d.nz + f - 1) / f, cy = (c->d.ny + f - 1) / f, cx = (c->d.nx + f - 1) / f;
   const Vol v{1, (cz + 3) / 4 * 4, (cy + 3) / 4 * 4, (cx + 3) / 4 * 4};
@@ -440,7 +451,8 @@ int ib3d_net_create(ib3d_net** out, uint64_t seed) {
   for (float** q : fb) ok = ok && cudaMalloc(q, n->nparam * sizeof(float)) == cudaSuccess;
   ok = ok && cudaMalloc(&n->wf, n->nparam * sizeof(bf16)) == cudaSuccess &&
        cudaMalloc(&n->wt, n->nparam * sizeof(bf16)) == cudaSuccess &&
-       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, (8 + 5 * (size_t)kNormBlocks) * sizeof(double)) == cudaSuccess;
+       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, (8 + 5 * (size_t)kNormBlocks) * sizeof(double)) == cudaSuccess &&
+       cudaMalloc(&n->d_err, sizeof(int)) == cudaSuccess && cudaMemset(n->d_err, 0, sizeof(int)) == cudaSuccess;
   if (!ok) {
     ib3d_net_destroy(n);
     return IB3D_ERR_MEMORY;
@@ -461,7 +473,7 @@ void ib3d_net_destroy(ib3d_net* n) {
   if (!n) return;
   if (n->st) cudaStreamSynchronize(n->st);
   free_buffers(n->buf);
-  void* ptrs[] = {n->p, n->g, n->m1, n->m2, n->wf, n->wt, n->ds_in, n->ds_t, n->d_loss, n->d_red};
+  void* ptrs[] = {n->p, n->g, n->m1, n->m2, n->wf, n->wt, n->ds_in, n->ds_t, n->d_loss, n->d_red, n->d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (n->st) cudaStreamDestroy(n->st);
@@ -511,7 +523,7 @@ int ib3d_net_loss_grad(ib3d_net* n, int B, int S, const float* x, const float* t
   NET_CUDA(n, cudaStreamSynchronize(n->st));
   cudaFree(dx);
   NET_CUDA(n, cudaGetLastError());
-  return IB3D_OK;
+  return check_conv(n);
 }
 
 // Reserves room for `capacity` training patches of edge S (S a multiple of 4).
@@ -599,6 +611,7 @@ int ib3d_net_train(ib3d_net* n, int steps, int batch, double lr, uint64_t seed, 
   }
   cudaFree(ids);
   NET_CUDA(n, cudaGetLastError());
+  if (int rc = check_conv(n)) return rc;
   if (last_loss) *last_loss = loss;
   return IB3D_OK;
 }

@@ -22,8 +22,10 @@ struct Act {
   int cs, co;
 };
 
+// err (device int) is set when a tensor-core wait gives up (it does not, unless the
+// device misbehaves); the host checks it after synchronising
 void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const float* bias, int relu, int sign, Act Y,
-          int N);
+          int N, int* err);
 void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW);
 void bias_grad(cudaStream_t st, long long M, Act dZ, int N, float* db);
 void relu_bwd(cudaStream_t st, long long M, int C, Act dY, Act Y);

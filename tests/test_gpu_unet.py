@@ -158,28 +158,34 @@ def test_capture_train_and_learned_warm_start(ib3d, grids):
     net.close()
 
 
-WEIGHTS = pathlib.Path(__file__).resolve().parent.parent / "ib3d-gpu_gb300" / "weights" / "unet_sphere256.f32"
+WEIGHTS_DIR = pathlib.Path(__file__).resolve().parent.parent / "ib3d-gpu_gb300" / "weights"
 
 
-def test_trained_network_saves_sweeps(ib3d, grids):
-    """What the trained network gains: on a held-out Reynolds number (275; trained
-    at 200/250/300/350) of the 256x192x192 sphere, the learned warm start needs
-    fewer SOR sweeps than the previous-correction warm start over steps 3-8 (the
-    network acts from step 3), both stopping at the same FP64 residual 1e-6 (pass
-    lengths adaptive so that the counts resolve small differences); drag and lift
-    agree within 1e-4."""
+def _networks():
+    import json
+    manifest = WEIGHTS_DIR / "networks.json"
+    return json.loads(manifest.read_text())["networks"] if manifest.exists() else {}
+
+
+@pytest.mark.parametrize("name", sorted(_networks()))
+def test_trained_network_saves_sweeps(ib3d, grids, name):
+    """What a trained network of the package gains: on a held-out Reynolds number
+    (275; trained at 200/250/300/350) of the 256x192x192 sphere, the learned warm
+    start needs fewer SOR sweeps than the previous-correction warm start over steps
+    3-8 (the network acts from step 3), both stopping at the same FP64 residual 1e-6
+    (pass lengths adaptive so that the counts resolve small differences); drag and
+    lift agree within 1e-4."""
     import dataclasses
     import importlib
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
-    if not WEIGHTS.exists():
-        pytest.skip("no trained weights in the package")
     net = ib3d.Net(seed=0)
-    net.set_params(np.fromfile(WEIGHTS, dtype="<f4"))
+    net.set_coarsening(int(_networks()[name]["coarsen"]))
+    net.set_params(np.fromfile(WEIGHTS_DIR / name, dtype="<f4"))
     cs = dataclasses.replace(grids.case("sphere256"), omega=1.99, eps=1e-6)
     ev = learned.evaluate(net, cs, 275.0, 8, inner_schedule=1)
     prev, lrn = ev["prev"], ev["learned"]
     saved = 1.0 - sum(lrn["sweeps"][2:]) / sum(prev["sweeps"][2:])
-    print(f"sweeps previous-correction {prev['sweeps']}, learned {lrn['sweeps']}: {100 * saved:.1f} % saved")
+    print(f"{name}: sweeps previous-correction {prev['sweeps']}, learned {lrn['sweeps']}: {100 * saved:.1f} % saved")
     assert saved > 0.0
     c0, c1 = np.array(prev["coef"][-1]), np.array(lrn["coef"][-1])
     assert abs((c1[0] + c1[1]) - (c0[0] + c0[1])) <= 1e-4 * abs(c0[0] + c0[1])
