@@ -46,17 +46,20 @@ METRIC = "steps/s at 256×192×192 sphere: learned+FP32 vs plain FP64, residual 
 # launch), per grid cell: the updated colour's r (4 B) and e (4 B read, 4 B written)
 # over half the cells, and the other colour's e (4 B) over the other half.
 BYTES_SOR32_LAUNCH = 8.0
-# DRAM bytes (read + written) per k_sor32p launch from one ncu capture of the
-# 256x192x192 workload (dram__bytes_read.sum + dram__bytes_write.sum, mean of a red
-# and a black launch; profiles/k_sor32p_sphere256.md): 60,741,760 B over 9,437,184
-# cells. Other workloads scale it by their cell count.
-DRAM_BYTES_PER_CELL_SOR32 = 60741760.0 / 9437184.0
+# DRAM bytes (read + written) per k_sor32p launch on the 256x192x192 workload from
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_sor32p_sphere256.md).
+# Warm: inside the sweep loop, caches as the previous pass left them (mean of four
+# launches, 22,946,560 B) -- the arrays stay in L2. Cold: caches flushed before the
+# launch (mean of a red and a black launch). Other workloads scale them by their cell
+# count.
+DRAM_BYTES_PER_CELL_SOR32 = 22946560.0 / 4 / 9437184.0
+DRAM_BYTES_PER_CELL_SOR32_COLD = 60741760.0 / 9437184.0
 BYTES_SOR64 = 25.0   # FP64 sweep: pc 8 r + b 8 + pc 8 w + flag 1
 
 
-def traffic_per_launch(cs) -> float:
-    """Measured DRAM bytes of one k_sor32p launch on this workload."""
-    return DRAM_BYTES_PER_CELL_SOR32 * cs.cells
+def traffic_per_launch(cs, cold: bool = False) -> float:
+    """Measured DRAM bytes of one k_sor32p launch on this workload (warm L2 unless cold)."""
+    return (DRAM_BYTES_PER_CELL_SOR32_COLD if cold else DRAM_BYTES_PER_CELL_SOR32) * cs.cells
 
 
 def package():
@@ -585,6 +588,10 @@ def main():
         "roofline": {"kernel": "k_sor32p (one colour pass of the FP32 red-black sweep, colour-packed)",
                      "bound": "hbm", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic_per_launch(cs),
+                     "traffic_cold": traffic_per_launch(cs, cold=True),
+                     "note": "the packed arrays (76 MB) stay in L2 inside the sweep loop: DRAM traffic is the "
+                             "warm-cache figure; the pass is bound by the L1 data pipe (71 % of peak while "
+                             "active), so frac is a rate of algorithmic bytes against the HBM peak",
                      "bytes_per_launch": BYTES_SOR32_LAUNCH * ncell, "cells": ncell,
                      "ms_per_launch": t_launch32 * 1e3,
                      "share_of_step": tm["sor32_ms"] / phase_total if phase_total else None,

@@ -211,6 +211,7 @@ int alloc_fields(ib3d_ctx* c) {
   if (c->d.nx % 2 == 0) {   // colour-packed arrays of the FP32 inner solve (even nx)
     c->packed_lp = packed_row_length(c->d.nx);
     const size_t np = (size_t)c->packed_lp * (size_t)c->d.NY2 * (size_t)c->d.NZ2;
+    if (np >= ((size_t)1 << 31)) return IB3D_ERR_TOO_LARGE;   // the sweep kernels use 32-bit offsets
     for (int q = 0; q < 2; ++q) {
       if (cudaMalloc(&c->ep[q], np * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
       if (cudaMalloc(&c->rp[q], np * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;

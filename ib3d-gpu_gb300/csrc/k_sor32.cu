@@ -58,59 +58,80 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
 
 // One colour pass. Block (32, kRows): a warp covers 32 float4 groups of one row
 // (j, k), so the row's colour phase is uniform across the warp; grid (ceil(nq/32),
-// ceil(ny/kRows), ceil(nz/kPlanes)) maps the rest without integer division. A thread
-// updates its four cells in kPlanes consecutive planes, carrying the other colour's
-// centre and upper plane over to the next plane instead of loading them again.
-constexpr int kPlanes = 2;
+// ceil(ny/kRows), ceil(nz/kPlanes)) maps the rest without integer division. A
+// thread updates its four cells in kPlanes consecutive planes, carrying the other
+// colour's centre and upper plane over to the next plane instead of loading them
+// again. The x neighbours beyond the thread's own four cells (the other colour's
+// last entry of group q-1 and first of group q+1) come from the neighbouring
+// lanes' centre values by shuffles; only the lanes at the ends of a warp's span
+// load them. The kernel is held to 64 registers (8 blocks of 128 threads per SM):
+// the pass is bound by the L1 data pipe with the arrays resident in L2, and the
+// warps that fit hide the load latency better than a longer unroll would.
+// Offsets are 32-bit (a packed array holds fewer than 2^31 entries, checked at
+// allocation).
+constexpr int kPlanes = 8;
 constexpr int kRows = 4;
 
 template <int COLOR>
-__global__ void __launch_bounds__(32 * kRows) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
-                                                float* __restrict__ e_own, const float* __restrict__ e_oth,
-                                                int Lp, float omega, float om1) {
+__global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
+                                                          float* __restrict__ e_own, const float* __restrict__ e_oth,
+                                                          int Lp, float omega, float om1) {
   // launched with programmatic dependent launch: the blocks may start while the
   // previous pass drains; wait for it (and its writes) before touching memory
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nq = ((d.nx >> 1) + 3) >> 2;
-  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int lane = threadIdx.x;
+  const int q = blockIdx.x * 32 + lane;
   const int j = blockIdx.y * kRows + threadIdx.y + 2;
   const int k0 = blockIdx.z * kPlanes + 2;
-  if (q >= nq || j > d.ny + 1) return;
-  const long long plane = (long long)(d.ny + 2) * Lp;
-  const long long sj = (long long)(j - 1) * Lp + 4 * q + 4;
-  const float ay0 = g.acy32[0][j - 1], ay1 = g.acy32[1][j - 1], ay2 = g.acy32[2][j - 1];
-  float4 ob = *reinterpret_cast<const float4*>(e_oth + (long long)(k0 - 2) * plane + sj);
-  float4 ox = *reinterpret_cast<const float4*>(e_oth + (long long)(k0 - 1) * plane + sj);
+  if (j <= d.ny + 1) {   // uniform across the warp, so the shuffles see all lanes
+    const bool active = q < nq;
+    const bool load_left = lane == 0, load_right = lane == 31 || q + 1 >= nq;
+    const int plane = (d.ny + 2) * Lp;
+    const int sj = (j - 1) * Lp + 4 * q + 4;
+    const float ay0 = g.acy32[0][j - 1], ay1 = g.acy32[1][j - 1], ay2 = g.acy32[2][j - 1];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ob = active ? *reinterpret_cast<const float4*>(e_oth + (k0 - 2) * plane + sj) : z4;
+    float4 ox = active ? *reinterpret_cast<const float4*>(e_oth + (k0 - 1) * plane + sj) : z4;
 #pragma unroll
-  for (int kk = 0; kk < kPlanes; ++kk) {
-    const int k = k0 + kk;
-    if (k > d.nz + 1) break;
-    const long long s0 = (long long)(k - 1) * plane + sj;
-    // does this row start (i = 2) with the colour being updated?
-    const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
-    const float4 rr = *reinterpret_cast<const float4*>(r_own + s0);
-    const float4 eo = *reinterpret_cast<const float4*>(e_own + s0);
-    const float4 os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
-    const float4 on = *reinterpret_cast<const float4*>(e_oth + s0 + Lp);
-    const float4 ot = *reinterpret_cast<const float4*>(e_oth + s0 + plane);
-    const float left = e_oth[s0 - 1], right = e_oth[s0 + 4];
-    const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
-    const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
-    const float sv[4] = {os.x, os.y, os.z, os.w};
-    const float nv[4] = {on.x, on.y, on.z, on.w};
-    const float bv[4] = {ob.x, ob.y, ob.z, ob.w};
-    const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
-    float ev[4] = {eo.x, eo.y, eo.z, eo.w};
-    const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
-    if (own_first)
-      update4<true>(rv, ev, oxa, sv, nv, bv, tv, g.axp[0][0][q], g.axp[0][1][q], g.axp[0][2][q], ay0, ay1, ay2,
-                    az0, az1, az2, omega, om1);
-    else
-      update4<false>(rv, ev, oxa, sv, nv, bv, tv, g.axp[1][0][q], g.axp[1][1][q], g.axp[1][2][q], ay0, ay1, ay2,
-                     az0, az1, az2, omega, om1);
-    *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
-    ob = ox;
-    ox = ot;
+    for (int kk = 0; kk < kPlanes; ++kk) {
+      const int k = k0 + kk;
+      if (k > d.nz + 1) break;
+      const int s0 = (k - 1) * plane + sj;
+      // does this row start (i = 2) with the colour being updated?
+      const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
+      float4 rr = z4, eo = z4, os = z4, on = z4, ot = z4;
+      if (active) {
+        rr = *reinterpret_cast<const float4*>(r_own + s0);
+        eo = *reinterpret_cast<const float4*>(e_own + s0);
+        os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
+        on = *reinterpret_cast<const float4*>(e_oth + s0 + Lp);
+        ot = *reinterpret_cast<const float4*>(e_oth + s0 + plane);
+      }
+      float left = __shfl_up_sync(0xffffffffu, ox.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, ox.x, 1);
+      if (active && load_left) left = e_oth[s0 - 1];
+      if (active && load_right) right = e_oth[s0 + 4];
+      const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
+      const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+      const float sv[4] = {os.x, os.y, os.z, os.w};
+      const float nv[4] = {on.x, on.y, on.z, on.w};
+      const float bv[4] = {ob.x, ob.y, ob.z, ob.w};
+      const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
+      float ev[4] = {eo.x, eo.y, eo.z, eo.w};
+      const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
+      if (active) {
+        const int sp = own_first ? 0 : 1;
+        const float4 a0 = g.axp[sp][0][q], a1 = g.axp[sp][1][q], a2 = g.axp[sp][2][q];
+        if (own_first)
+          update4<true>(rv, ev, oxa, sv, nv, bv, tv, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
+        else
+          update4<false>(rv, ev, oxa, sv, nv, bv, tv, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
+        *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+      }
+      ob = ox;
+      ox = ot;
+    }
   }
   // the next pass may launch now; its griddepcontrol.wait still waits for this grid
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -153,12 +174,13 @@ void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  const float* r = c->rp[color];
+  float* e = c->ep[color];
+  const float* o = c->ep[1 - color];
   if (color == 0)
-    cudaLaunchKernelEx(&cfg, k_sor32p<0>, d, c->g, (const float*)c->rp[0], c->ep[0], (const float*)c->ep[1],
-                       c->packed_lp, omega, om1);
+    cudaLaunchKernelEx(&cfg, k_sor32p<0>, d, c->g, r, e, o, c->packed_lp, omega, om1);
   else
-    cudaLaunchKernelEx(&cfg, k_sor32p<1>, d, c->g, (const float*)c->rp[1], c->ep[1], (const float*)c->ep[0],
-                       c->packed_lp, omega, om1);
+    cudaLaunchKernelEx(&cfg, k_sor32p<1>, d, c->g, r, e, o, c->packed_lp, omega, om1);
 }
 
 void launch_accumulate_packed(ib3d_ctx* c) {
