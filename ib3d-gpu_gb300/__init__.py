@@ -31,7 +31,7 @@ ERR_IO = -9
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
 PREC_FP64, PREC_FP32DC = 0, 1
 WARM_ZERO, WARM_PREV, WARM_LEARNED = 0, 1, 2
-INNER_FIXED, INNER_ADAPTIVE = 0, 1
+INNER_FIXED, INNER_ADAPTIVE, INNER_TAIL = 0, 1, 2
 MESH_GMSH, MESH_GAMBIT = 0, 1
 OUTLET_ZERO_GRADIENT, OUTLET_CONVECTIVE = 0, 1
 MOMENTUM_EULER, MOMENTUM_AB2 = 0, 1

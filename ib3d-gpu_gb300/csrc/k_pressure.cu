@@ -478,7 +478,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   if (rc) return rc;
   if (!packed) IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
   long long sweeps = 0, outer = 0;
-  int batch = inner;
+  int batch = inner, prev_batch = inner;
   double prev_res = 0.0;
   for (;;) {
     {
@@ -499,7 +499,18 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       const double cap = std::log(1e-4) / rate;
       batch = (int)std::min(std::max(std::min(1.08 * need + 8.0, cap), 16.0), 65536.0);
     }
+    if (P.inner_schedule == IB3D_INNER_TAIL) {
+      // passes of `inner` sweeps; the one the last pass's rate says will reach eps is cut
+      // to the sweeps it needs (a prediction that falls short costs one more pass)
+      batch = inner;
+      if (outer > 0 && res > 0.0 && res < prev_res) {
+        const double rate = std::log(res / prev_res) / prev_batch;
+        const double need = std::log(P.eps / res) / rate;
+        batch = (int)std::min(std::max(1.08 * need + 8.0, 16.0), (double)inner);
+      }
+    }
     if (sweeps + batch > P.max_sweeps) batch = (int)std::max(1ll, P.max_sweeps - sweeps);
+    prev_batch = batch;
     prev_res = res;
     {
       PhaseScope ps(c, PH_SOR32);

@@ -58,6 +58,7 @@ extern "C" {
 /* ib3d_params.inner_schedule */
 #define IB3D_INNER_FIXED 0
 #define IB3D_INNER_ADAPTIVE 1
+#define IB3D_INNER_TAIL 2
 /* ib3d_params.outlet */
 #define IB3D_OUTLET_ZERO_GRADIENT 0
 #define IB3D_OUTLET_CONVECTIVE 1
@@ -84,7 +85,9 @@ typedef struct ib3d_params {
                              the first pass runs inner_sweeps, later passes as many as the measured
                              residual reduction per sweep predicts are needed to reach eps (at most
                              four decades per FP32 solve), so fewer FP64 residual passes run and the
-                             last pass overshoots less */
+                             last pass overshoots less; IB3D_INNER_TAIL: every pass runs inner_sweeps
+                             except the last, which runs as many as the previous pass's reduction
+                             per sweep predicts are needed to reach eps (+8 % and 8 sweeps) */
   int32_t outlet;         /* IB3D_OUTLET_ZERO_GRADIENT (the reference's active outlet,
                              subBoundaryConditions.f90:149-151) or IB3D_OUTLET_CONVECTIVE (Orlanski,
                              the commented :153-155, with the speed uc of calculateUc,
