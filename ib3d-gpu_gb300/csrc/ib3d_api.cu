@@ -482,7 +482,7 @@ void ib3d_destroy(ib3d_ctx* c) {
   void* ptrs[] = {c->d_tables, c->d_tables32, c->d_fast, c->d_axp, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
-                  c->hist[0], c->hist[1], c->r_hist, c->resi[0], c->resi[1], c->resi[2]};
+                  c->hist[0], c->hist[1], c->r_hist, c->d_norm, c->d_norm_part, c->resi[0], c->resi[1], c->resi[2]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -780,6 +780,11 @@ int ib3d_enable_history(ib3d_ctx* c) {
     IB3D_CUDA(c, cudaMalloc(&c->r_hist, (size_t)c->d.n3 * sizeof(float)));
     IB3D_CUDA(c, cudaMemsetAsync(c->r_hist, 0, (size_t)c->d.n3 * sizeof(float), c->st));
   }
+  if (!c->d_norm) {
+    IB3D_CUDA(c, cudaMalloc(&c->d_norm, sizeof(NetNorm)));
+    IB3D_CUDA(c, cudaMemsetAsync(c->d_norm, 0, sizeof(NetNorm), c->st));   // valid = 0
+    IB3D_CUDA(c, cudaMalloc(&c->d_norm_part, (size_t)net_norm_blocks(c) * 5 * sizeof(double)));
+  }
   c->hist_valid = 0;
   return IB3D_OK;
 }
@@ -829,6 +834,7 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
     st.solve_seconds = ms * 1e-3;
     std::memcpy(&st.divmax, &h[0], sizeof(double));
     std::memcpy(&st.derr_std_st, &h[1], sizeof(double));
+    if (c->prm.warm_start == IB3D_WARM_LEARNED) net_note_failure(c);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

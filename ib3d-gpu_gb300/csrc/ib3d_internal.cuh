@@ -52,6 +52,15 @@ struct Grid1D {
   const double *corx, *cory, *corz;
 };
 
+// RMS over the fluid cells of each network input -- pc^{n-1} = p^{n-1} - p^{n-2},
+// b/dt, p^{n-1}, r/diag -- and their reciprocals; valid = 0 while any of them is 0
+// (then the network is not used and pc keeps the previous correction).
+struct NetNorm {
+  double s1, s2, s3, s4;
+  double r1, r2, r3, r4;
+  int valid;
+};
+
 // Shared control block of the sweep loop; lives in device memory.
 struct SolveCtl {
   unsigned long long upd;     // max |delta pc| of the running sweep (bit pattern, >= 0)
@@ -170,6 +179,10 @@ struct ib3d_ctx {
   // by the diagonal (FP32, padded layout, 0 off the fluid cells), kept for the
   // network and for capture
   float* r_hist = nullptr;
+  // the network inputs' normalisation of this step (device; written with r_hist) and
+  // the per-block partial sums it is reduced from
+  ib3d::NetNorm* d_norm = nullptr;
+  double* d_norm_part = nullptr;
   ib3d_net* net = nullptr;
 
   // phase timers (ib3d_timers_*) and the launch counter
@@ -215,11 +228,17 @@ int run_velocity_forcing(ib3d_ctx* c);
 int run_pressure_forcing(ib3d_ctx* c);
 int run_stress(ib3d_ctx* c, int first, double coef[4]);
 
-// unet.cu: pc = the attached network's prediction; nonzero when not available yet
 int run_move_body(ib3d_ctx* c, double dx, double dy, double dz);
+// unet.cu: pc = the attached network's prediction; nonzero when not available yet
 int net_predict_pc(ib3d_ctx* c);
-// k_fast.cu: r_hist = ((b/dt) - A pc) / diag(A) for the current pc
+// unet.cu: after a step's synchronisation, records a convolution that gave up (the
+// step then used the previous correction) in the network's error string
+void net_note_failure(ib3d_ctx* c);
+// k_fast.cu: r_hist = ((b/dt) - A pc) / diag(A) for the current pc, and the inputs'
+// normalisation (NetNorm) from it, both on the device
 void net_hist_residual(ib3d_ctx* c);
+// blocks of the k_hist_residual launch (one partial-sum row each)
+long long net_norm_blocks(const ib3d_ctx* c);
 
 // error helper: records the message and returns IB3D_ERR_CUDA
 int cuda_fail(ib3d_ctx* c, cudaError_t e, const char* where);

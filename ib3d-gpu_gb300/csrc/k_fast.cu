@@ -125,11 +125,124 @@ __global__ void __launch_bounds__(kBlock) k_hist_residual(Dims d, Grid1D g, cons
   r[tid] = out;
 }
 
+// Sums over the fluid cells of (h1-h2)^2, (b/dt)^2, h1^2, (r/diag)^2 and their
+// count, for the network inputs' RMS. Grid (ceil(nx/256), ny, ceil(nz/kNormPlanes)):
+// a thread accumulates kNormPlanes cells of one column in FP64 (one FMA per sum and
+// cell), the warp adds its threads' sums in FP32 and the block its warps' in FP64,
+// one partial row per block, in a fixed order.
+constexpr int kNormPlanes = 8;
+__global__ void __launch_bounds__(kBlock) k_norm_sums(Dims d, const unsigned char* __restrict__ cell,
+                                                      const double* __restrict__ h1, const double* __restrict__ h2,
+                                                      const double* __restrict__ bdt, const float* __restrict__ r,
+                                                      double* __restrict__ partial) {
+  static_assert(kBlock == 256, "the block reduction below assumes 8 warps");
+  __shared__ double sm[8][5];
+  const int i = blockIdx.x * kBlock + threadIdx.x + 2, j = blockIdx.y + 2, k0 = blockIdx.z * kNormPlanes + 2;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  float a3 = 0.f, a4 = 0.f;
+  if (i <= d.nx + 1) {
+#pragma unroll
+    for (int kk = 0; kk < kNormPlanes; ++kk) {
+      const int k = k0 + kk;
+      if (k > d.nz + 1) break;
+      const long long o = d.at(i, j, k);
+      if (cell[o] == 0) {
+        const double p1 = h1[o], b = bdt[o], dp = p1 - h2[o];
+        const float rr = r[o];
+        a0 = fma(dp, dp, a0);
+        a1 = fma(b, b, a1);
+        a2 = fma(p1, p1, a2);
+        a3 = fmaf(rr, rr, a3);
+        a4 += 1.f;
+      }
+    }
+  }
+  float q[5] = {(float)a0, (float)a1, (float)a2, a3, a4};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    float x = q[c];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if (lane == 0) sm[wid][c] = (double)x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double x = 0.0;
+    for (int w = 0; w < 8; ++w) x += sm[w][threadIdx.x];
+    const size_t b = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    partial[b * 5 + threadIdx.x] = x;
+  }
+}
+
+// Adds the per-block partial sums in a fixed order (each thread a strided set of
+// rows, four at a time, then a tree over the threads), so the normalisation does not
+// depend on scheduling, and writes NetNorm.
+constexpr int kNormThreads = 1024;
+__global__ void __launch_bounds__(kNormThreads) k_norm_final(const double* __restrict__ partial, int nblocks,
+                                                             NetNorm* __restrict__ out) {
+  __shared__ double sm[5][kNormThreads];
+  const int t = threadIdx.x;
+  double x[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  int b = t;
+  for (; b + 3 * kNormThreads < nblocks; b += 4 * kNormThreads) {
+    double v[4][5];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) v[u][c] = partial[(size_t)(b + u * kNormThreads) * 5 + c];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) x[c] += v[u][c];
+  }
+  for (; b < nblocks; b += kNormThreads)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) x[c] += partial[(size_t)b * 5 + c];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) sm[c][t] = x[c];
+  __syncthreads();
+  for (int s = kNormThreads / 2; s > 0; s >>= 1) {
+    if (t < s)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) sm[c][t] += sm[c][t + s];
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double tot[5] = {sm[0][0], sm[1][0], sm[2][0], sm[3][0], sm[4][0]};
+    NetNorm nm{};
+    nm.valid = tot[0] > 0.0 && tot[1] > 0.0 && tot[2] > 0.0 && tot[3] > 0.0 && tot[4] > 0.0;
+    if (nm.valid) {
+      nm.s1 = sqrt(tot[0] / tot[4]);
+      nm.s2 = sqrt(tot[1] / tot[4]);
+      nm.s3 = sqrt(tot[2] / tot[4]);
+      nm.s4 = sqrt(tot[3] / tot[4]);
+      nm.r1 = 1.0 / nm.s1;
+      nm.r2 = 1.0 / nm.s2;
+      nm.r3 = 1.0 / nm.s3;
+      nm.r4 = 1.0 / nm.s4;
+    }
+    *out = nm;
+  }
+}
+
 }  // namespace
+
+static dim3 norm_grid(const Dims& d) {
+  return dim3((unsigned)((d.nx + kBlock - 1) / kBlock), (unsigned)d.ny,
+              (unsigned)((d.nz + kNormPlanes - 1) / kNormPlanes));
+}
+
+long long net_norm_blocks(const ib3d_ctx* c) {
+  const dim3 g = norm_grid(c->d);
+  return (long long)g.x * g.y * g.z;
+}
 
 void net_hist_residual(ib3d_ctx* c) {
   k_hist_residual<<<nblk(c->d.n3), kBlock, 0, c->st>>>(c->d, c->g, c->bdt, c->pc, c->cell, c->r_hist);
-  c->launches += 1;
+  const dim3 g = norm_grid(c->d);
+  k_norm_sums<<<g, kBlock, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt, c->r_hist, c->d_norm_part);
+  k_norm_final<<<1, kNormThreads, 0, c->st>>>(c->d_norm_part, (int)(g.x * g.y * g.z), c->d_norm);
+  c->launches += 3;
 }
 
 void launch_divergence_fast(ib3d_ctx* c, bool zero_pc) {

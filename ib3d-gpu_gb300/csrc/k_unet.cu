@@ -10,10 +10,11 @@
 // tensor cores (tcgen05.mma kind::f16, BF16 operands from shared memory, FP32
 // accumulator in tensor memory): rows are 128 voxels of a block, columns the
 // output channels, and the reduction runs over 27 taps x input channels in steps of
-// 16 channels. The threads gather each step's A tile (the 128 voxels' neighbours,
-// 16 channels each) and B tile (the weights) into a double-buffered shared-memory
-// stage in the canonical no-swizzle K-major layout, one thread issues the MMA, and
-// a tcgen05.commit to the stage's mbarrier frees it for the step after next. The
+// 16 channels. The threads gather four steps' A tiles (the 128 voxels' neighbours,
+// 16 channels each) and B tiles (the weights) into one of two shared-memory stages
+// in the canonical no-swizzle K-major layout, one thread issues the stage's four
+// MMAs, and a tcgen05.commit to the stage's mbarrier frees it for the stage after
+// next; the next stage's loads are in flight meanwhile. The
 // same kernel computes the input gradient with mirrored taps and transposed
 // weights. Weight gradients are reduced on the CUDA cores in FP32.
 #include <cuda_bf16.h>
@@ -62,16 +63,33 @@ __device__ __forceinline__ void decode(long long m, const Vol& v, int& b, int& z
 
 // Y[v][n] = act( sum_{tap,k} X[v + sign*off(tap)][k] * Wt[n][tap][k] + bias[n] ),
 // N output channels (a multiple of 16, at most 128). Block: 128 threads, 128
-// consecutive voxels; D in tensor memory (128 lanes x N FP32 columns). Every wait
-// is bounded and decided for the whole block: a barrier that does not complete sets
-// *err, and the kernel still waits (bounded) for its issued MMAs before it frees the
-// tensor memory.
+// consecutive voxels; D in tensor memory (128 lanes x N FP32 columns).
+//
+// The reduction runs in steps of 16 (tap, channel) pairs, kSub steps per stage: a
+// stage is kSub A tiles (128 x 16) and kSub B tiles (N x 16) in shared memory, and
+// one thread issues its kSub MMAs back to back and commits them to the stage's
+// mbarrier. Two stages alternate, and every thread loads the next stage's
+// neighbour values into registers before the current stage's MMAs are issued, so
+// the global-load latency overlaps the tensor-core work; the registers go to shared
+// memory once the MMAs that last read that stage have completed.
+//
+// Every wait is bounded and decided for the whole block: a barrier that does not
+// complete sets *err, and the kernel still waits (bounded) for its issued MMAs
+// before it frees the tensor memory.
+constexpr int kSub = 4;
+
+template <int N>
+constexpr size_t conv_smem_bytes() {
+  return (size_t)2 * kSub * (128 * 16 + N * 16) * sizeof(bf16);
+}
+
 template <int N>
 __global__ void __launch_bounds__(128) k_conv3(Vol vol, Act X, int K, const bf16* __restrict__ Wt,
                                                const float* __restrict__ bias, int relu, int sign, Act Y, int* err) {
   static_assert(N % 16 == 0 && N >= 16 && N <= 128, "tcgen05 N");
-  __shared__ __align__(128) bf16 sA[2][128 * 16];
-  __shared__ __align__(128) bf16 sB[2][N * 16];
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  bf16* sA = reinterpret_cast<bf16*>(smraw);             // [2][kSub][128 * 16]
+  bf16* sB = sA + 2 * kSub * 128 * 16;                     // [2][kSub][N * 16]
   __shared__ __align__(8) unsigned long long bar[3];
   __shared__ unsigned tmem_base;
   constexpr unsigned kCols = N <= 32 ? 32 : (N <= 64 ? 64 : 128);   // power of two >= N
@@ -96,56 +114,96 @@ __global__ void __launch_bounds__(128) k_conv3(Vol vol, Act X, int K, const bf16
   if (vok) decode(m, vol, vb, vz, vy, vx);
   // instruction descriptor: D FP32, A and B BF16, both K-major, N, M = 128
   const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((128u >> 4) << 24);
-  const int kchunks = K / 16, steps = 27 * kchunks;
+  const int kchunks = K / 16, steps = 27 * kchunks, nst = (steps + kSub - 1) / kSub;
+  const int g = t >> 3, rr = t & 7;   // core-matrix row group and row of this thread's A (and B) row
+  uint4 ra[kSub][2], rb[kSub][2];
+  // registers of stage q: this voxel's neighbour and this thread's weight row, per step
+  auto gather = [&](int q) {
+#pragma unroll
+    for (int j = 0; j < kSub; ++j) {
+      const int s = q * kSub + j;
+      ra[j][0] = ra[j][1] = rb[j][0] = rb[j][1] = make_uint4(0, 0, 0, 0);
+      if (s < steps) {
+        const int tap = s / kchunks, kc = (s % kchunks) * 16;
+        const int z = vz + sign * (tap / 9 - 1), y = vy + sign * ((tap / 3) % 3 - 1), x = vx + sign * (tap % 3 - 1);
+        if (vok && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W) {
+          const long long sv = (((long long)vb * vol.D + z) * vol.H + y) * vol.W + x;
+          const uint4* src = reinterpret_cast<const uint4*>(X.p + sv * X.cs + X.co + kc);
+          ra[j][0] = src[0];
+          ra[j][1] = src[1];
+        }
+        if (t < N) {
+          const uint4* w = reinterpret_cast<const uint4*>(Wt + ((size_t)t * 27 + tap) * K + kc);
+          rb[j][0] = w[0];
+          rb[j][1] = w[1];
+        }
+      }
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int j = 0; j < kSub; ++j) {
+      char* a = reinterpret_cast<char*>(sA + (buf * kSub + j) * 128 * 16);
+      *reinterpret_cast<uint4*>(a + (g * 2 + 0) * 128 + rr * 16) = ra[j][0];
+      *reinterpret_cast<uint4*>(a + (g * 2 + 1) * 128 + rr * 16) = ra[j][1];
+      if (t < N) {
+        char* b = reinterpret_cast<char*>(sB + (buf * kSub + j) * N * 16);
+        *reinterpret_cast<uint4*>(b + (g * 2 + 0) * 128 + rr * 16) = rb[j][0];
+        *reinterpret_cast<uint4*>(b + (g * 2 + 1) * 128 + rr * 16) = rb[j][1];
+      }
+    }
+  };
+  gather(0);
+  store(0);
   unsigned phase[2] = {0, 0};
   bool ok = true;
-  for (int s = 0; s < steps; ++s) {
-    const int st = s & 1;
-    if (s >= 2) {   // the MMA that read this stage two steps ago must be done
-      ok = __syncthreads_and(mbar_wait(&bar[st], phase[st], 1 << 20)) != 0;
-      phase[st] ^= 1;
-      if (!ok) break;
-    }
-    const int tap = s / kchunks, kc = (s % kchunks) * 16;
-    const int dz = sign * (tap / 9 - 1), dy = sign * ((tap / 3) % 3 - 1), dx = sign * (tap % 3 - 1);
-    uint4 h0 = make_uint4(0, 0, 0, 0), h1 = make_uint4(0, 0, 0, 0);
-    const int z = vz + dz, y = vy + dy, x = vx + dx;
-    if (vok && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W) {
-      const long long sv = (((long long)vb * vol.D + z) * vol.H + y) * vol.W + x;
-      const uint4* src = reinterpret_cast<const uint4*>(X.p + sv * X.cs + X.co + kc);
-      h0 = src[0];
-      h1 = src[1];
-    }
-    const int g = t >> 3, rr = t & 7;   // core-matrix row group and row of this thread's A row
-    char* a = reinterpret_cast<char*>(sA[st]);
-    *reinterpret_cast<uint4*>(a + (g * 2 + 0) * 128 + rr * 16) = h0;
-    *reinterpret_cast<uint4*>(a + (g * 2 + 1) * 128 + rr * 16) = h1;
-    if (t < N) {
-      const uint4* w = reinterpret_cast<const uint4*>(Wt + ((size_t)t * 27 + tap) * K + kc);
-      char* bsm = reinterpret_cast<char*>(sB[st]);
-      *reinterpret_cast<uint4*>(bsm + (g * 2 + 0) * 128 + rr * 16) = w[0];
-      *reinterpret_cast<uint4*>(bsm + (g * 2 + 1) * 128 + rr * 16) = w[1];
-    }
+  for (int q = 0; q < nst; ++q) {
+    const int buf = q & 1;
+    if (q + 1 < nst) gather(q + 1);   // in flight while this stage's MMAs are issued and run
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // make the stage visible to the tensor core
     __syncthreads();
     if (t == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const unsigned long long ad = smem_desc(sA[st], 128, 256), bd = smem_desc(sB[st], 128, 256);
-      asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                   " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                   :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(s > 0 ? 1u : 0u) : "memory");
+#pragma unroll
+      for (int j = 0; j < kSub; ++j) {
+        const int s = q * kSub + j;
+        if (s < steps) {
+          const unsigned long long ad = smem_desc(sA + (buf * kSub + j) * 128 * 16, 128, 256);
+          const unsigned long long bd = smem_desc(sB + (buf * kSub + j) * N * 16, 128, 256);
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                       :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(s > 0 ? 1u : 0u) : "memory");
+        }
+      }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                   :: "r"(smem_addr(&bar[st])) : "memory");
+                   :: "r"(smem_addr(&bar[buf])) : "memory");
+    }
+    if (q + 1 < nst) {
+      const int nb = buf ^ 1;
+      if (q >= 1) {   // stage nb was last read by the MMAs of stage q - 1
+        ok = __syncthreads_and(mbar_wait(&bar[nb], phase[nb], 1 << 20)) != 0;
+        phase[nb] ^= 1;
+        if (!ok) break;
+      }
+      store(nb);
     }
   }
   // a commit after the last MMA arrives once every MMA of this thread is done
   if (t == 0)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                  :: "r"(smem_addr(&bar[2])) : "memory");
-  const bool done = __syncthreads_and(mbar_wait(&bar[2], 0, 1 << 20)) != 0;
+  bool done = __syncthreads_and(mbar_wait(&bar[2], 0, 1 << 20)) != 0;
+  if (ok && done) {
+    // the last one or two stages' own arrivals, so that none is left pending at exit
+    for (int q = nst >= 2 ? nst - 2 : 0; q < nst; ++q) {
+      const int b = q & 1;
+      done = __syncthreads_and(mbar_wait(&bar[b], phase[b], 1 << 20)) != 0 && done;
+      phase[b] ^= 1;
+    }
+  }
   if (!ok || !done) {
     if (t == 0) atomicExch(err, 1);
-    if (!done) mbar_wait(&bar[2], 0, 1 << 20);   // let the issued MMAs finish before freeing the columns
+    mbar_wait(&bar[2], 0, 1 << 20);   // let the issued MMAs finish before freeing the columns
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
@@ -390,16 +448,28 @@ __global__ void k_cast_conv_weights(int N, int K, const float* __restrict__ w, b
 
 // ------------------------------------------------------------ launch helpers
 
+template <int N>
+void launch_conv3(cudaStream_t st, unsigned nb, const Vol& vol, Act X, int K, const bf16* W, const float* bias,
+                  int relu, int sign, Act Y, int* err) {
+  constexpr size_t smem = conv_smem_bytes<N>();
+  static bool attr = false;   // the stages need more than the default 48 KB of dynamic shared memory
+  if (!attr) {
+    cudaFuncSetAttribute(k_conv3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_conv3<N><<<nb, 128, smem, st>>>(vol, X, K, W, bias, relu, sign, Y, err);
+}
+
 void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const float* bias, int relu, int sign, Act Y,
           int N, int* err) {
   const long long M = vol.voxels();
   const unsigned nb = (unsigned)((M + 127) / 128);
   switch (N) {
-    case 16: k_conv3<16><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
-    case 32: k_conv3<32><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
-    case 48: k_conv3<48><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
-    case 64: k_conv3<64><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
-    case 96: k_conv3<96><<<nb, 128, 0, st>>>(vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 16: launch_conv3<16>(st, nb, vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 32: launch_conv3<32>(st, nb, vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 48: launch_conv3<48>(st, nb, vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 64: launch_conv3<64>(st, nb, vol, X, K, W, bias, relu, sign, Y, err); break;
+    case 96: launch_conv3<96>(st, nb, vol, X, K, W, bias, relu, sign, Y, err); break;
     default: break;
   }
 }

@@ -73,7 +73,6 @@ struct ib3d_net {
   float* ds_t = nullptr;   // [patch][S^3]
   double* d_loss = nullptr;
   int* d_err = nullptr;    // set by a convolution whose tensor-core wait gave up
-  double* d_red = nullptr; // normalisation sums [5] and per-block partials (from [8])
 };
 
 namespace {
@@ -204,62 +203,15 @@ void cast_weights(ib3d_net* n) {
 
 // ------------------------------------------------------------- data kernels
 
-// RMS inputs over fluid cells: sums of (h1-h2)^2, (b/dt)^2, h1^2, r^2 and the
-// fluid count. kNormBlocks blocks stride over the cells and write one partial sum
-// per block; k_norm_final adds the partials in block order, so the result does not
-// depend on scheduling (and needs no atomics on five contended addresses).
-constexpr int kNormBlocks = 1216;
-__global__ void __launch_bounds__(256) k_norm_sums(Dims d, const unsigned char* __restrict__ cell,
-                                                   const double* __restrict__ h1, const double* __restrict__ h2,
-                                                   const double* __restrict__ bdt, const float* __restrict__ r,
-                                                   double* __restrict__ partial) {
-  __shared__ double sm[8][5];
-  double s[5] = {0, 0, 0, 0, 0};
-  const unsigned n = (unsigned)d.nx * (unsigned)d.ny * (unsigned)d.nz;
-  for (unsigned tid = blockIdx.x * blockDim.x + threadIdx.x; tid < n; tid += gridDim.x * blockDim.x) {
-    const int i = (int)(tid % (unsigned)d.nx) + 2;
-    const unsigned t = tid / (unsigned)d.nx;
-    const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
-    const long long o = d.at(i, j, k);
-    if (cell[o] == 0) {
-      const double dp = h1[o] - h2[o];
-      const double rr = (double)r[o];
-      s[0] += dp * dp; s[1] += bdt[o] * bdt[o]; s[2] += h1[o] * h1[o]; s[3] += rr * rr; s[4] += 1.0;
-    }
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int q = 0; q < 5; ++q) {
-    double x = s[q];
-    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-    if (lane == 0) sm[wid][q] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < 5) {
-    double x = 0.0;
-    for (int w = 0; w < 8; ++w) x += sm[w][threadIdx.x];
-    partial[(size_t)blockIdx.x * 5 + threadIdx.x] = x;
-  }
-}
-
-__global__ void k_norm_final(const double* __restrict__ partial, int nblocks, double* __restrict__ sums) {
-  if (threadIdx.x >= 5) return;
-  double x = 0.0;
-  for (int b = 0; b < nblocks; ++b) x += partial[(size_t)b * 5 + threadIdx.x];
-  sums[threadIdx.x] = x;
-}
-
-struct Norm {
-  double s1, s2, s3, s4;   // RMS of each input over the fluid cells
-  double r1, r2, r3, r4;   // their reciprocals (inputs are scaled by products)
-};
-
 // Input channels of one cell (see the file header); channels kInputs..15 are zero.
+// The difference of the pressures is taken in FP64; the scaling in FP32 (sc holds
+// the reciprocal RMS values r1..r4 of NetNorm).
 __device__ __forceinline__ void cell_inputs(long long o, const double* h1, const double* h2, const double* bdt,
-                                            const float* r, Norm nm, float in[kInputs]) {
-  in[0] = (float)((h1[o] - h2[o]) * nm.r1);
-  in[1] = (float)(bdt[o] * nm.r2);
-  in[2] = (float)(h1[o] * nm.r3);
-  in[3] = r[o] * (float)nm.r4;
+                                            const float* r, const float sc[kInputs], float in[kInputs]) {
+  in[0] = (float)(h1[o] - h2[o]) * sc[0];
+  in[1] = (float)bdt[o] * sc[1];
+  in[2] = (float)h1[o] * sc[2];
+  in[3] = r[o] * sc[3];
 }
 
 // Inputs of one coarse voxel: the average of cell_inputs over the f^3 fine cells it
@@ -267,7 +219,8 @@ __device__ __forceinline__ void cell_inputs(long long o, const double* h1, const
 // non-fluid cells count as zero inputs.
 __device__ __forceinline__ void coarse_inputs(const Dims& d, const unsigned char* cell, int f, int i0, int j0,
                                               int k0, const double* h1, const double* h2, const double* bdt,
-                                              const float* r, Norm nm, float in[kInputs]) {
+                                              const float* r, const NetNorm& nm, float in[kInputs]) {
+  const float sc[kInputs] = {(float)nm.r1, (float)nm.r2, (float)nm.r3, (float)nm.r4};
   float acc[kInputs] = {};
   int n = 0;
   for (int dz = 0; dz < f; ++dz)
@@ -279,7 +232,7 @@ __device__ __forceinline__ void coarse_inputs(const Dims& d, const unsigned char
         const long long o = d.at(i, j, k);
         if (cell[o] != 0) continue;
         float c[kInputs];
-        cell_inputs(o, h1, h2, bdt, r, nm, c);
+        cell_inputs(o, h1, h2, bdt, r, sc, c);
 #pragma unroll
         for (int q = 0; q < kInputs; ++q) acc[q] += c[q];
       }
@@ -292,13 +245,14 @@ __device__ __forceinline__ void coarse_inputs(const Dims& d, const unsigned char
 // extents rounded up to multiples of 4, zero outside the domain.
 __global__ void k_pack_domain(Dims d, Vol v, int f, const unsigned char* __restrict__ cell,
                               const double* __restrict__ h1, const double* __restrict__ h2,
-                              const double* __restrict__ bdt, const float* __restrict__ r, Norm nm,
-                              bf16* __restrict__ in0) {
+                              const double* __restrict__ bdt, const float* __restrict__ r,
+                              const NetNorm* __restrict__ nmp, bf16* __restrict__ in0) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= v.voxels()) return;
   const int x = (int)(m % v.W), y = (int)((m / v.W) % v.H), z = (int)(m / ((long long)v.W * v.H));
   float in[kInputs] = {};
-  if (f * x < d.nx && f * y < d.ny && f * z < d.nz)
+  const NetNorm nm = *nmp;
+  if (nm.valid && f * x < d.nx && f * y < d.ny && f * z < d.nz)
     coarse_inputs(d, cell, f, 2 + f * x, 2 + f * y, 2 + f * z, h1, h2, bdt, r, nm, in);
   bf16* dst = in0 + m * 16;
 #pragma unroll
@@ -306,12 +260,16 @@ __global__ void k_pack_domain(Dims d, Vol v, int f, const unsigned char* __restr
 }
 
 // pc = (p^{n-1} - p^{n-2}) + s1 * out(coarse voxel of the cell) on fluid cells, 0
-// elsewhere (the coarse prediction taken back piecewise constant).
+// elsewhere (the coarse prediction taken back piecewise constant). Without a valid
+// normalisation, or after a convolution gave up (err), pc is left as it is: the
+// previous correction.
 __global__ void k_unpack_domain(Dims d, Vol v, int f, const float* __restrict__ out,
                                 const unsigned char* __restrict__ cell, const double* __restrict__ h1,
-                                const double* __restrict__ h2, double s1, double* __restrict__ pc) {
+                                const double* __restrict__ h2, const NetNorm* __restrict__ nmp,
+                                const int* __restrict__ err, double* __restrict__ pc) {
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= (unsigned)d.n3) return;
+  if (tid >= (unsigned)d.n3 || !nmp->valid || *err != 0) return;
+  const double s1 = nmp->s1;
   const int i = (int)(tid % (unsigned)d.NX2);
   const unsigned t = tid / (unsigned)d.NX2;
   const int j = (int)(t % (unsigned)d.NY2), k = (int)(t / (unsigned)d.NY2);
@@ -328,10 +286,11 @@ __global__ void k_unpack_domain(Dims d, Vol v, int f, const float* __restrict__ 
 __global__ void k_capture(Dims d, int S, int f, int i0, int j0, int k0, const double* __restrict__ h1,
                           const double* __restrict__ h2, const double* __restrict__ bdt,
                           const float* __restrict__ r, const double* __restrict__ pc,
-                          const unsigned char* __restrict__ cell, Norm nm, bf16* __restrict__ din,
-                          float* __restrict__ dt) {
+                          const unsigned char* __restrict__ cell, const NetNorm* __restrict__ nmp,
+                          bf16* __restrict__ din, float* __restrict__ dt) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= (long long)S * S * S) return;
+  const NetNorm nm = *nmp;
   const int x = (int)(m % S), y = (int)((m / S) % S), z = (int)(m / ((long long)S * S));
   const int ci = i0 + f * x, cj = j0 + f * y, ck = k0 + f * z;
   float in[kInputs];
@@ -371,26 +330,6 @@ __global__ void k_set_input(long long M, const float* __restrict__ x, bf16* __re
   for (int c = 0; c < kInputs; ++c) in0[m * 16 + c] = __float2bfloat16(x[m * kInputs + c]);
 }
 
-int norm_for(ib3d_net* n, ib3d_ctx* c, Norm* nm) {
-  k_norm_sums<<<kNormBlocks, 256, 0, c->st>>>(c->d, c->cell, c->hist[0], c->hist[1], c->bdt, c->r_hist,
-                                               n->d_red + 8);
-  k_norm_final<<<1, 32, 0, c->st>>>(n->d_red + 8, kNormBlocks, n->d_red);
-  double h[5];
-  NET_CUDA(n, cudaMemcpyAsync(h, n->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
-  NET_CUDA(n, cudaStreamSynchronize(c->st));
-  for (int q = 0; q < 5; ++q)
-    if (!(h[q] > 0)) return IB3D_ERR_ARG;
-  nm->s1 = std::sqrt(h[0] / h[4]);
-  nm->s2 = std::sqrt(h[1] / h[4]);
-  nm->s3 = std::sqrt(h[2] / h[4]);
-  nm->s4 = std::sqrt(h[3] / h[4]);
-  nm->r1 = 1.0 / nm->s1;
-  nm->r2 = 1.0 / nm->s2;
-  nm->r3 = 1.0 / nm->s3;
-  nm->r4 = 1.0 / nm->s4;
-  return IB3D_OK;
-}
-
 }  // namespace
 
 namespace ib3d {
@@ -398,10 +337,9 @@ namespace ib3d {
 // history or the normalisation is not available yet; pc is then left unchanged).
 int net_predict_pc(ib3d_ctx* c) {
   ib3d_net* n = c->net;
-  if (!n || c->hist_valid < 2) return 1;
-  Norm nm;
-  if (norm_for(n, c, &nm) != IB3D_OK) return 1;
-  if (check_conv(n) != IB3D_OK) return 1;   // a failed convolution earlier: keep the previous correction
+  if (!n || c->hist_valid < 2 || !c->d_norm) return 1;
+  // no host synchronisation here: the normalisation (k_hist_residual, this step) and
+  // the convolutions' status are read on the device by the pack and unpack kernels
   const int f = n->coarsen;
   const int cz = (c->d.nz + f - 1) / f, cy = (c->d.ny + f - 1) / f, cx = (c->d.nx + f - 1) / f;
   const Vol v{1, (cz + 3) / 4 * 4, (cy + 3) / 4 * 4, (cx + 3) / 4 * 4};
@@ -410,14 +348,22 @@ int net_predict_pc(ib3d_ctx* c) {
   int rc = ensure_buffers(n, v, false);
   if (rc) { n->st = saved; return rc; }
   k_pack_domain<<<(unsigned)((v.voxels() + 255) / 256), 256, 0, c->st>>>(c->d, v, f, c->cell, c->hist[0],
-                                                                         c->hist[1], c->bdt, c->r_hist, nm,
+                                                                         c->hist[1], c->bdt, c->r_hist, c->d_norm,
                                                                          n->buf.in0);
   forward(n);
   k_unpack_domain<<<(unsigned)((c->d.n3 + 255) / 256), 256, 0, c->st>>>(c->d, v, f, n->buf.out, c->cell,
-                                                                        c->hist[0], c->hist[1], nm.s1, c->pc);
+                                                                        c->hist[0], c->hist[1], c->d_norm, n->d_err,
+                                                                        c->pc);
   n->st = saved;
-  c->launches += 18;
+  c->launches += 17;
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+void net_note_failure(ib3d_ctx* c) {
+  if (!c->net) return;
+  int h = 0;
+  if (cudaMemcpy(&h, c->net->d_err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && h)
+    c->net->err = "ib3d_net: a tensor-core wait timed out; the steps since used the previous correction";
 }
 }  // namespace ib3d
 
@@ -451,7 +397,7 @@ int ib3d_net_create(ib3d_net** out, uint64_t seed) {
   for (float** q : fb) ok = ok && cudaMalloc(q, n->nparam * sizeof(float)) == cudaSuccess;
   ok = ok && cudaMalloc(&n->wf, n->nparam * sizeof(bf16)) == cudaSuccess &&
        cudaMalloc(&n->wt, n->nparam * sizeof(bf16)) == cudaSuccess &&
-       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess && cudaMalloc(&n->d_red, (8 + 5 * (size_t)kNormBlocks) * sizeof(double)) == cudaSuccess &&
+       cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess &&
        cudaMalloc(&n->d_err, sizeof(int)) == cudaSuccess && cudaMemset(n->d_err, 0, sizeof(int)) == cudaSuccess;
   if (!ok) {
     ib3d_net_destroy(n);
@@ -473,7 +419,7 @@ void ib3d_net_destroy(ib3d_net* n) {
   if (!n) return;
   if (n->st) cudaStreamSynchronize(n->st);
   free_buffers(n->buf);
-  void* ptrs[] = {n->p, n->g, n->m1, n->m2, n->wf, n->wt, n->ds_in, n->ds_t, n->d_loss, n->d_red, n->d_err};
+  void* ptrs[] = {n->p, n->g, n->m1, n->m2, n->wf, n->wt, n->ds_in, n->ds_t, n->d_loss, n->d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (n->st) cudaStreamDestroy(n->st);
@@ -560,8 +506,9 @@ int ib3d_net_capture(ib3d_net* n, ib3d_ctx* c, int npatches, uint64_t seed) {
   if (c->hist_valid < 2) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: fewer than two previous pressures");
   const int S = n->S, f = n->coarsen, F = S * f;   // F fine cells per patch edge
   if (F > c->d.nx || F > c->d.ny || F > c->d.nz) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: patch larger than grid");
-  Norm nm;
-  if (norm_for(n, c, &nm) != IB3D_OK) return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: zero normalisation");
+  NetNorm nm{};
+  if (!c->d_norm || cudaMemcpy(&nm, c->d_norm, sizeof(nm), cudaMemcpyDeviceToHost) != cudaSuccess || !nm.valid)
+    return fail(n, IB3D_ERR_ARG, "ib3d_net_capture: zero normalisation");
   std::mt19937_64 rng(seed);
   const size_t per = (size_t)S * S * S;
   for (int q = 0; q < npatches && n->count < n->cap; ++q) {
@@ -569,7 +516,7 @@ int ib3d_net_capture(ib3d_net* n, ib3d_ctx* c, int npatches, uint64_t seed) {
     const int j0 = 2 + (int)(rng() % (uint64_t)(c->d.ny - F + 1));
     const int k0 = 2 + (int)(rng() % (uint64_t)(c->d.nz - F + 1));
     k_capture<<<(unsigned)((per + 255) / 256), 256, 0, c->st>>>(c->d, S, f, i0, j0, k0, c->hist[0], c->hist[1],
-                                                                c->bdt, c->r_hist, c->pc, c->cell, nm,
+                                                                c->bdt, c->r_hist, c->pc, c->cell, c->d_norm,
                                                                 n->ds_in + n->count * per * kInputs,
                                                                 n->ds_t + n->count * per);
     n->count++;
