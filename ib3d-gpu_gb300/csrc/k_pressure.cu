@@ -516,12 +516,16 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       PhaseScope ps(c, PH_SOR32);
       c->launches += 2 * batch;
       for (int q = 0; q < batch; ++q) {
+        // the solve's first sweeps at relaxation 1 (smooth_sweeps): Gauss-Seidel damps the
+        // high-frequency error that the over-relaxed sweeps barely touch
+        const bool smooth = outer == 0 && q < P.smooth_sweeps;
+        const float w = smooth ? 1.0f : om, w1 = smooth ? 0.0f : om1;
         if (packed) {
-          launch_sor32_packed(c, 0, om, om1);
-          launch_sor32_packed(c, 1, om, om1);
+          launch_sor32_packed(c, 0, w, w1);
+          launch_sor32_packed(c, 1, w, w1);
         } else {
-          k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
-          k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, om, om1);
+          k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, w, w1);
+          k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, w, w1);
         }
       }
     }

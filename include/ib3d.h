@@ -94,6 +94,12 @@ typedef struct ib3d_params {
                              subCalculateuc.f90:2-38, taken after each step's pressure forcing) */
   int32_t momentum;       /* IB3D_MOMENTUM_EULER (nsMomentum) or IB3D_MOMENTUM_AB2: ib3d_step uses
                              nsMomentumAB (subNavierStokes.f90:1128-1628) after the first step */
+  int32_t smooth_sweeps;  /* FP32 form only: the first pass of each pressure solve begins with this
+                             many red-black sweeps at relaxation 1 (Gauss-Seidel), counted among the
+                             pass's sweeps. Over-relaxed sweeps (omega near 2) damp the
+                             high-frequency part of the initial error by only |omega - 1| per sweep;
+                             a few Gauss-Seidel sweeps remove what a coarse-grid guess (the learned
+                             warm start) or the new right-hand side adds there. 0: none */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */
