@@ -96,20 +96,24 @@ SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
 WEIGHTS_DIR = ROOT / "ib3d-gpu_gb300" / "weights"
 
 
-def load_net(pkg, name: str = ""):
-    """The trained warm-start network (networks.json's default, or `name`), or None
-    when no weights are present."""
+def load_net(pkg, name: str = "", coarsen: int = 4):
+    """The trained warm-start network (networks.json's default, or `name` there), or
+    None when no weights are present. A `name` with a directory part is a weights file
+    outside the package, run at coarsening `coarsen`."""
     import numpy as np
-    manifest = WEIGHTS_DIR / "networks.json"
-    if not manifest.exists():
-        return None
-    info = json.loads(manifest.read_text())
-    name = name or info["default"]
-    path = WEIGHTS_DIR / name
+    if os.sep in name:
+        path, f = pathlib.Path(name), coarsen
+    else:
+        manifest = WEIGHTS_DIR / "networks.json"
+        if not manifest.exists():
+            return None
+        info = json.loads(manifest.read_text())
+        name = name or info["default"]
+        path, f = WEIGHTS_DIR / name, int(info["networks"].get(name, {}).get("coarsen", coarsen))
     if not path.exists():
         return None
     net = pkg.Net(seed=0)
-    net.set_coarsening(int(info["networks"][name]["coarsen"]))
+    net.set_coarsening(f)
     w = np.fromfile(path, dtype="<f4")
     if w.size != net.nparams:
         raise SystemExit(f"{path}: {w.size} weights, the network has {net.nparams}")
@@ -118,20 +122,22 @@ def load_net(pkg, name: str = ""):
     return net
 
 
-def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2) -> dict:
-    """Generates snapshots (4 perturbed runs at Re 200/250/300/350, 24 steps, 8 random
-    patches of 64^3 coarse voxels = 128^3 cells per step from step 3), trains with Adam
-    for `seconds` (batch 8, lr 1e-3 then 2e-4 for the last 30 %), writes the FP32
-    weights, and compares sweeps on a held-out Re 275 run (adaptive pass lengths, so
-    that the counts resolve differences below 256 sweeps)."""
+def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200.0, 250.0, 300.0, 350.0),
+              steps: int = 24, patches: int = 8) -> dict:
+    """Generates snapshots (perturbed runs at the given Reynolds numbers -- by default
+    Re 200/250/300/350 --, `steps` steps each, `patches` random patches of 128^3 cells
+    per step from step 3), trains with Adam for `seconds` (batch 8, lr 1e-3 then 2e-4
+    for the last 30 %), writes the FP32 weights, and compares sweeps on a held-out Re
+    275 run (adaptive pass lengths, so that the counts resolve differences below 256
+    sweeps)."""
     import dataclasses
     import numpy as np
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
     net = pkg.Net(seed=0)
     net.set_coarsening(coarsen)
-    net.reserve(128 // coarsen, 4 * 24 * 8)     # patches of 128^3 cells
+    net.reserve(128 // coarsen, len(reynolds) * (steps - 2) * patches)     # patches of 128^3 cells
     net.coarsen = coarsen
-    gen = learned.generate(net, cs, [200.0, 250.0, 300.0, 350.0], 24, 8)
+    gen = learned.generate(net, cs, list(reynolds), steps, patches)
     fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
     before = fit()
     t0, steps = time.perf_counter(), 0
@@ -438,6 +444,9 @@ def main():
                          "its weights to this file")
     ap.add_argument("--train-seconds", type=float, default=300.0)
     ap.add_argument("--coarsen", type=int, default=4, help="coarsening of the network trained by --train-net")
+    ap.add_argument("--train-re", default="200,250,300,350", help="Reynolds numbers of --train-net's runs")
+    ap.add_argument("--train-steps", type=int, default=24, help="steps of each --train-net run")
+    ap.add_argument("--train-patches", type=int, default=8, help="patches captured per step by --train-net")
     ap.add_argument("--weights", default="", help="weights file in ib3d-gpu_gb300/weights (default: networks.json's)")
     ap.add_argument("--moving", action="store_true",
                     help="instead of the step benchmark: the transversely oscillating sphere "
@@ -457,7 +466,8 @@ def main():
     if args.train_net:
         if dist.rank == 0:
             print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds,
-                                       args.coarsen)), flush=True)
+                                       args.coarsen, [float(r) for r in args.train_re.split(",")],
+                                       args.train_steps, args.train_patches)), flush=True)
         dist.close()
         return
     if args.moving:
@@ -520,7 +530,7 @@ def main():
     arms = set(args.arms.split(","))
     # Headline: FP32 sweeps in FP64 defect correction with the learned warm start (the
     # trained network in the package); without weights, the previous-correction warm start.
-    net = load_net(pkg, args.weights) if "learned" in arms else None
+    net = load_net(pkg, args.weights, args.coarsen) if "learned" in arms else None
     head_mode = dict(FAST, warm_start=pkg.WARM_LEARNED) if net is not None else FAST
     clocks = Clocks(dist.local)
     fast = run_arm(pkg, cs, head_mode, warmup, args.steps, dist, timers=True, clocks=clocks, net=net)
