@@ -387,6 +387,40 @@ def run_poisson(pkg, n: int) -> dict:
     return out
 
 
+def compare_fp64(pkg, cs, steps: int, net=None) -> dict:
+    """The mixed-precision form (the bench's FP32 arm, learned warm start when a
+    network is given) against the plain FP64 path over the same `steps` steps, both to
+    the same FP64 residual: drag and lift of every step, and u, v, w, p after the last
+    step (largest difference relative to the field's largest magnitude)."""
+    import numpy as np
+    fast = dict(FAST, warm_start=pkg.WARM_LEARNED) if net is not None else dict(FAST)
+    a = pkg.setup_case(cs, **PLAIN)
+    b = pkg.setup_case(cs, **fast)
+    if net is not None:
+        b.attach_net(net)
+    rows = []
+    for q in range(1, steps + 1):
+        sa, ca = a.step(q == 1)
+        sb, cb = b.step(q == 1)
+        cd, cd_ref = cb[0] + cb[1], ca[0] + ca[1]
+        cl, cl_ref = cb[2] + cb[3], ca[2] + ca[3]
+        rows.append({"step": q, "sweeps_fp64": sa["sweeps"], "sweeps_fp32": sb["sweeps"],
+                     "drag_rel": abs(cd - cd_ref) / abs(cd_ref),
+                     "lift_abs": abs(cl - cl_ref), "lift_rel_to_drag": abs(cl - cl_ref) / abs(cd_ref)})
+    fields = {}
+    for f in ("u", "v", "w", "p"):
+        x, y = a.get_field(f), b.get_field(f)
+        fields[f] = float(np.max(np.abs(x - y)) / np.max(np.abs(x)))
+    a.close()
+    b.close()
+    return {"workload": f"{cs.name} {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]}, Re {cs.re:g}, {steps} steps, "
+                        f"residual <= {cs.eps:g}",
+            "mode": "learned warm start" if net is not None else "previous-correction warm start",
+            "worst_drag_rel": max(r["drag_rel"] for r in rows),
+            "worst_lift_rel_to_drag": max(r["lift_rel_to_drag"] for r in rows),
+            "fields_max_rel_after_last_step": fields, "steps": rows}
+
+
 def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, freq: float = 0.2) -> dict:
     """The body oscillates as y(t) = amp sin(2 pi freq t): before every step the nodes
     move (ib3d_move_body, surface velocity y'(t)), the search re-tags a box around
@@ -452,6 +486,9 @@ def main():
                     help="instead of the step benchmark: the transversely oscillating sphere "
                          "(y = 0.2 sin(2 pi 0.2 t), search every step) on --case (default sphere384), "
                          "FP32 form and plain FP64")
+    ap.add_argument("--compare-fp64", type=int, default=0,
+                    help="instead of the benchmark: this many steps of the FP32 form (learned warm start) "
+                         "against the plain FP64 path: drag/lift and field differences")
     ap.add_argument("--set", default="",
                     help="comma-separated key=value overrides of the FP32-sweep arm's solver parameters")
     ap.add_argument("--arms", default="fast,learned,plain,e2e,cpu",
@@ -484,6 +521,12 @@ def main():
     if args.poisson:
         if dist.rank == 0:
             print(json.dumps(run_poisson(pkg, args.poisson)), flush=True)
+        dist.close()
+        return
+    if args.compare_fp64:
+        if dist.rank == 0:
+            print(json.dumps(compare_fp64(pkg, workload(pkg, args.case), args.compare_fp64,
+                                          load_net(pkg, args.weights, args.coarsen))), flush=True)
         dist.close()
         return
     cs = workload(pkg, args.case)
