@@ -155,6 +155,37 @@ def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200
                            for k, v in ev.items()}}
 
 
+def train_moving(pkg, cs, out: str, seconds: float, weights: str = "", coarsen: int = 4, steps: int = 200,
+                 patches: int = 8) -> dict:
+    """Fine-tunes a trained network on the moving sphere: captures `patches` patches of
+    128^3 cells per step from steps 3..`steps` of a run whose initial u carries a seeded
+    1 % perturbation (FP32 form, previous-correction warm start), then trains with Adam
+    for `seconds` from the given weights (lr 2e-4, then 5e-5 for the last 30 %) and
+    writes the FP32 weights."""
+    import numpy as np
+    learned = importlib.import_module("ib3d_gpu_gb300.learned")
+    net = load_net(pkg, weights, coarsen)
+    if net is None:
+        raise SystemExit("train-moving: no network to start from")
+    net.reserve(128 // net.coarsen, (steps - 2) * patches)
+    t0 = time.perf_counter()
+    gen = run_moving(pkg, cs, FAST, 0, steps, perturb=0.01, seed=1, capture=(net, patches))
+    t_gen = time.perf_counter() - t0
+    fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
+    before = fit()
+    t0, done = time.perf_counter(), 0
+    while time.perf_counter() - t0 < seconds:
+        lr = 2e-4 if time.perf_counter() - t0 < 0.7 * seconds else 5e-5
+        learned.train(net, 100, batch=8, lr=lr, chunk=100, seed=done)
+        done += 100
+    after = fit()
+    pathlib.Path(out).parent.mkdir(parents=True, exist_ok=True)
+    net.get_params().astype("<f4").tofile(out)
+    return {"weights": str(out), "patches": net.dataset_size(), "generate_s": t_gen,
+            "generate_sweeps_per_step": gen["sweeps_per_step"], "adam_steps": done,
+            "train_s": time.perf_counter() - t0, "training_set_loss": [before, after]}
+
+
 # ------------------------------------------------------------------ clocks
 
 class Clocks:
@@ -421,14 +452,28 @@ def compare_fp64(pkg, cs, steps: int, net=None) -> dict:
             "fields_max_rel_after_last_step": fields, "steps": rows}
 
 
-def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, freq: float = 0.2) -> dict:
+def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, freq: float = 0.2, net=None,
+               perturb: float = 0.0, seed: int = 0, capture=None) -> dict:
     """The body oscillates as y(t) = amp sin(2 pi freq t): before every step the nodes
     move (ib3d_move_body, surface velocity y'(t)), the search re-tags a box around
     the new position, then the step runs. Timed with CUDA events on the library
-    stream around the timed steps (move, search and step together)."""
+    stream around the timed steps (move, search and step together). With `net` the
+    solve starts from the network's guess; `perturb` adds a seeded relative
+    perturbation to the initial u; `capture` = (network, patches) captures training
+    patches of every step from step 3."""
     import math
+    import numpy as np
     import torch
+    if net is not None:
+        mode = dict(mode, warm_start=pkg.WARM_LEARNED)
     s = pkg.setup_case(cs, **mode)
+    if net is not None:
+        s.attach_net(net)
+    if capture is not None:
+        s.enable_history()
+    if perturb:
+        u = s.get_field("u")
+        s.set_field("u", u + perturb * np.random.default_rng(seed).standard_normal(u.shape))
     w = 2.0 * math.pi * freq
     y = 0.0
     stream = torch.cuda.ExternalStream(s.stream())
@@ -449,6 +494,8 @@ def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, f
         st, coef = s.step(n == 1)
         if n > warmup:
             sweeps.append(st["sweeps"])
+        if capture is not None and n >= 3:
+            capture[0].capture(s, capture[1], seed=1000 * seed + n)
     e1.record(stream)
     e1.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
@@ -478,6 +525,10 @@ def main():
                          "its weights to this file")
     ap.add_argument("--train-seconds", type=float, default=300.0)
     ap.add_argument("--coarsen", type=int, default=4, help="coarsening of the network trained by --train-net")
+    ap.add_argument("--train-moving", default="",
+                    help="instead of the benchmark: fine-tune the network given by --weights (default: "
+                         "networks.json's) on the first --train-steps steps of a perturbed run of the moving "
+                         "sphere (--case, default sphere384) and write its weights to this file")
     ap.add_argument("--train-re", default="200,250,300,350", help="Reynolds numbers of --train-net's runs")
     ap.add_argument("--train-steps", type=int, default=24, help="steps of each --train-net run")
     ap.add_argument("--train-patches", type=int, default=8, help="patches captured per step by --train-net")
@@ -507,14 +558,27 @@ def main():
                                        args.train_steps, args.train_patches)), flush=True)
         dist.close()
         return
+    if args.train_moving:
+        if dist.rank == 0:
+            mcs = workload(pkg, args.case if args.case != "sphere256" else "sphere384")
+            print(json.dumps(train_moving(pkg, mcs, args.train_moving, args.train_seconds, args.weights, args.coarsen,
+                                          args.train_steps, args.train_patches)), flush=True)
+        dist.close()
+        return
     if args.moving:
         if dist.rank == 0:
             mcs = workload(pkg, args.case if args.case != "sphere256" else "sphere384")
             out = {"workload": f"{mcs.name} {mcs.shape[0]}x{mcs.shape[1]}x{mcs.shape[2]}, Re {mcs.re:g}, moving sphere "
                                "y = 0.2 sin(2 pi 0.2 t), search every step, residual <= 1e-6",
-                   "fp32": run_moving(pkg, mcs, FAST, warmup, args.steps),
-                   "plain_fp64": run_moving(pkg, mcs, PLAIN, warmup, max(1, args.plain_steps // 2))}
+                   "fp32": run_moving(pkg, mcs, FAST, warmup, args.steps)}
+            mnet = load_net(pkg, args.weights, args.coarsen)
+            if mnet is not None:
+                out["fp32_learned"] = run_moving(pkg, mcs, FAST, warmup, args.steps, net=mnet)
+                out["fp32_learned"]["weights"] = mnet.weights
+            out["plain_fp64"] = run_moving(pkg, mcs, PLAIN, warmup, max(1, args.plain_steps // 2))
             out["speedup"] = out["fp32"]["value"] / out["plain_fp64"]["value"]
+            if mnet is not None:
+                out["speedup_learned"] = out["fp32_learned"]["value"] / out["plain_fp64"]["value"]
             print(json.dumps(out), flush=True)
         dist.close()
         return
