@@ -186,6 +186,19 @@ void fast_tables(const std::vector<double>& d, int n, int axis, const std::vecto
     put(23, m, 2.0 / (hs * (0.5 * (dm + dp))));
     put(24, m, 2.0 / (hs * (0.5 * (dm + dl))));
     put(25, m, 1.0 / dm);
+    // third-order upwind folded: adv*sa*ra + |adv|*sk*rk = adv * sum_q (ca*ra +- ck*rk) q,
+    // + for adv >= 0 and - for adv < 0, for the own-axis family (ra, rk of tables 1, 2)
+    // and the transverse one (tables 3, 4)
+    const double ro[2] = {1.0 / (cc[axis][5][m] * dp), 1.0 / (cc[3 + axis][5][m] * (0.5 * (dm + dp)))};
+    const double rk[2] = {1.0 / (2.0 * cc[axis][11][m] * dm), 1.0 / (2.0 * cc[3 + axis][11][m] * (0.5 * (dm + dl)))};
+    for (int h = 0; h < 2; ++h) {
+      const int fam = h == 0 ? axis : 3 + axis;
+      for (int q = 0; q < 5; ++q) {
+        const double a = cc[fam][q][m] * ro[h], k = cc[fam][6 + q][m] * rk[h];
+        put(26 + 10 * h + q, m, a + k);
+        put(31 + 10 * h + q, m, a - k);
+      }
+    }
   }
 }
 

@@ -22,7 +22,7 @@
 namespace ib3d {
 
 constexpr int kBlock = 256;
-constexpr int kFastTables = 26;   // 1-D tables per axis of the fast kernels (k_momentum_fast.cu, k_fast.cu)
+constexpr int kFastTables = 46;   // 1-D tables per axis of the fast kernels (k_momentum_fast.cu, k_fast.cu)
 
 // Index helpers: 1-based Fortran (i,j,k) into the padded column-major array.
 struct Dims {

@@ -19,6 +19,9 @@
 //   21 cna  2/((d[m]+d[m+1]) d[m+1])   22 cnb 2/((d[m]+d[m+1]) d[m])       node diffusion
 //   23 cha  2/(0.5(2d[m]+d[m+1]+d[m-1]) 0.5(d[m]+d[m+1]))  24 chb  .../0.5(d[m]+d[m-1])  half diffusion
 //   25 rd   1/d[m]                                reciprocal spacing (divergence, k_fast.cu)
+//   26..30  third-order upwind of the own-axis family for adv >= 0: ca[q]*ran + ck[q]*rkn, q = 0..4
+//   31..35  the same for adv < 0: ca[q]*ran - ck[q]*rkn
+//   36..45  the same for the transverse family with rah, rkh
 #include "ib3d_internal.cuh"
 
 namespace ib3d {
@@ -33,14 +36,16 @@ struct Ft {
   }
 };
 
-// third-order upwind with reciprocal tables
-template <int FAM>
-__device__ __forceinline__ double up3f(const Grid1D& g, double adv, int m, double q2, double q1, double q0,
-                                       double qm1, double qm2, double ra, double rk) {
-  const double* const* c = g.cc[FAM];
-  const double sa = fma(c[4][m], qm2, fma(c[3][m], qm1, fma(c[2][m], q0, fma(c[1][m], q1, c[0][m] * q2))));
-  const double sk = fma(c[10][m], qm2, fma(c[9][m], qm1, fma(c[8][m], q0, fma(c[7][m], q1, c[6][m] * q2))));
-  return fma(adv * sa, ra, fabs(adv) * sk * rk);
+// third-order upwind: adv * ca.q * ra + |adv| * ck.q * rk = adv * (ca*ra +- ck*rk).q, the
+// folded coefficients read from the tables of adv's sign (OWN: the component's own
+// axis, else a transverse one)
+template <bool OWN>
+__device__ __forceinline__ double up3f(const Ft& F, int axis, int m, double adv, double q2, double q1, double q0,
+                                       double qm1, double qm2) {
+  const int b = (OWN ? 26 : 36) + (adv < 0.0 ? 5 : 0);
+  const double s = fma(F(axis, b + 4, m), qm2,
+                       fma(F(axis, b + 3, m), qm1, fma(F(axis, b + 2, m), q0, fma(F(axis, b + 1, m), q1, F(axis, b, m) * q2))));
+  return adv * s;
 }
 
 // first-order upwind; base = 5 (node) or 13 (half)
@@ -85,9 +90,9 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
     const double win = 0.5 * (fma(wx, W[o] - W[o + sx], W[o + sx]) + fma(wx, W[o - sz] - W[o + sx - sz], W[o + sx - sz]));
     double cx, cy, cz;
     if (i != 2 && i < nx && j != 2 && j < ny + 1 && k != 2 && k < nz + 1 && noib) {
-      cx = up3f<0>(g, u0, i, U[o + 2 * sx], U[o + sx], u0, U[o - sx], U[o - 2 * sx], F(0, 1, i), F(0, 2, i));
-      cy = up3f<4>(g, vin, j, U[o + 2 * sy], U[o + sy], u0, U[o - sy], U[o - 2 * sy], F(1, 3, j), F(1, 4, j));
-      cz = up3f<5>(g, win, k, U[o + 2 * sz], U[o + sz], u0, U[o - sz], U[o - 2 * sz], F(2, 3, k), F(2, 4, k));
+      cx = up3f<true>(F, 0, i, u0, U[o + 2 * sx], U[o + sx], u0, U[o - sx], U[o - 2 * sx]);
+      cy = up3f<false>(F, 1, j, vin, U[o + 2 * sy], U[o + sy], u0, U[o - sy], U[o - 2 * sy]);
+      cz = up3f<false>(F, 2, k, win, U[o + 2 * sz], U[o + sz], u0, U[o - sz], U[o - 2 * sz]);
     } else {
       cx = up1f(F, 0, 5, i, u0, U[o - sx], u0, U[o + sx]);
       cy = up1f(F, 1, 13, j, vin, U[o - sy], u0, U[o + sy]);
@@ -108,9 +113,9 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
     const double win = 0.5 * (fma(wy, W[o] - W[o + sy], W[o + sy]) + fma(wy, W[o - sz] - W[o + sy - sz], W[o + sy - sz]));
     double cx, cy, cz;
     if (i != 2 && i < nx + 1 && j != 2 && j < ny && k != 2 && k < nz + 1 && noib) {
-      cx = up3f<3>(g, uin, i, V[o + 2 * sx], V[o + sx], v0, V[o - sx], V[o - 2 * sx], F(0, 3, i), F(0, 4, i));
-      cy = up3f<1>(g, v0, j, V[o + 2 * sy], V[o + sy], v0, V[o - sy], V[o - 2 * sy], F(1, 1, j), F(1, 2, j));
-      cz = up3f<5>(g, win, k, V[o + 2 * sz], V[o + sz], v0, V[o - sz], V[o - 2 * sz], F(2, 3, k), F(2, 4, k));
+      cx = up3f<false>(F, 0, i, uin, V[o + 2 * sx], V[o + sx], v0, V[o - sx], V[o - 2 * sx]);
+      cy = up3f<true>(F, 1, j, v0, V[o + 2 * sy], V[o + sy], v0, V[o - sy], V[o - 2 * sy]);
+      cz = up3f<false>(F, 2, k, win, V[o + 2 * sz], V[o + sz], v0, V[o - sz], V[o - 2 * sz]);
     } else {
       cx = up1f(F, 0, 13, i, uin, V[o - sx], v0, V[o + sx]);
       cy = up1f(F, 1, 5, j, v0, V[o - sy], v0, V[o + sy]);
@@ -131,9 +136,9 @@ __global__ void __launch_bounds__(128) k_momentum_fast(Dims d, Grid1D g, const d
     const double vin = 0.5 * (fma(wz, V[o] - V[o + sz], V[o + sz]) + fma(wz, V[o - sy] - V[o - sy + sz], V[o - sy + sz]));
     double cx, cy, cz;
     if (i != 2 && i < nx + 1 && j != 2 && j < ny + 1 && k != 2 && k < nz && noib) {
-      cx = up3f<3>(g, uin, i, W[o + 2 * sx], W[o + sx], w0, W[o - sx], W[o - 2 * sx], F(0, 3, i), F(0, 4, i));
-      cy = up3f<4>(g, vin, j, W[o + 2 * sy], W[o + sy], w0, W[o - sy], W[o - 2 * sy], F(1, 3, j), F(1, 4, j));
-      cz = up3f<2>(g, w0, k, W[o + 2 * sz], W[o + sz], w0, W[o - sz], W[o - 2 * sz], F(2, 1, k), F(2, 2, k));
+      cx = up3f<false>(F, 0, i, uin, W[o + 2 * sx], W[o + sx], w0, W[o - sx], W[o - 2 * sx]);
+      cy = up3f<false>(F, 1, j, vin, W[o + 2 * sy], W[o + sy], w0, W[o - sy], W[o - 2 * sy]);
+      cz = up3f<true>(F, 2, k, w0, W[o + 2 * sz], W[o + sz], w0, W[o - sz], W[o - 2 * sz]);
     } else {
       cx = up1f(F, 0, 13, i, uin, W[o - sx], w0, W[o + sx]);
       cy = up1f(F, 1, 13, j, vin, W[o - sy], w0, W[o + sy]);
