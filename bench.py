@@ -9,12 +9,16 @@ reference's full step (momentum predictor, boundary conditions, ghost-point
 forcing, red-black SOR pressure solve with relaxation 1.99 to an FP64 residual
 L-inf <= 1e-6, pressure/velocity correction, drag/lift).
 
-value  = steps/s of the fast form: FP32 red-black sweeps inside an FP64
-         defect-correction loop, warm-started from the previous step's
-         correction, stopped at the same FP64 residual as the plain path.
+value  = steps/s of the headline form: FP32 red-black sweeps inside an FP64
+         defect-correction loop (passes of 512 sweeps, the last one cut to what
+         the measured rate needs, the first six at relaxation 1), warm-started
+         by the trained U-Net of ib3d-gpu_gb300/weights, stopped at the same FP64
+         residual as the plain path. `fp32_previous_correction` is the same form
+         warm-started from the previous step's correction (the network's
+         fallback).
 plain  = steps/s of the plain FP64 path (reference arithmetic, zero initial
          correction) over the same physical steps.
-e2e    = the fast form through the C ABI with host buffers: the state is
+e2e    = the headline form through the C ABI with host buffers: the state is
          uploaded from pinned host memory at the start of the timed region and
          every step downloads u,v,w,ut,vt,wt,p to pinned host memory, as the
          reference's per-step `update host` (main.f90:55) does.
