@@ -90,9 +90,11 @@ def workload(pkg, name: str):
 # either warm start (1.99-1.999 scanned; 1.9932 and 1.994 need 3-10 % more); passes of 512
 # sweeps with the last one cut to what the measured rate needs (IB3D_INNER_TAIL); the solve's first
 # 6 sweeps at relaxation 1 (smooth_sweeps: 4, 6 and 10 need 6.2, 7.0 and 7.4 % fewer sweeps with the
-# learned guess than none, 2-3 % with the previous correction)
+# learned guess than none, 2-3 % with the previous correction), then 32 sweeps whose relaxation
+# rises linearly to omega_inner (ramp_sweeps: 1.0 % fewer sweeps with the learned guess, 1.9 % with
+# the previous correction; 4-12 less, 64-256 worse)
 FAST = dict(precision=1, warm_start=1, criterion=1, inner_sweeps=512, inner_schedule=2, omega_inner=1.9937,
-            smooth_sweeps=6, sweep_kernel=0, max_sweeps=400000)
+            smooth_sweeps=6, ramp_sweeps=32, sweep_kernel=0, max_sweeps=400000)
 PLAIN = dict(precision=0, warm_start=0, criterion=1, check_every=8, max_sweeps=400000)
 SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
 # U-Net weights trained on the GPU by this library's own kernels (bench.py --train-net);

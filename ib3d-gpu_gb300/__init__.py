@@ -52,7 +52,8 @@ class Params(C.Structure):
                 ("max_sweeps", C.c_int64), ("criterion", C.c_int32), ("precision", C.c_int32),
                 ("warm_start", C.c_int32), ("check_every", C.c_int32), ("inner_sweeps", C.c_int32),
                 ("sweep_kernel", C.c_int32), ("omega_inner", C.c_double), ("inner_schedule", C.c_int32),
-                ("outlet", C.c_int32), ("momentum", C.c_int32), ("smooth_sweeps", C.c_int32)]
+                ("outlet", C.c_int32), ("momentum", C.c_int32), ("smooth_sweeps", C.c_int32),
+                ("ramp_sweeps", C.c_int32)]
 
 
 class SolveStats(C.Structure):

@@ -258,7 +258,7 @@ bool valid_params(const ib3d_params* p) {
          (p->precision == 0 || p->precision == 1) && (p->warm_start >= 0 && p->warm_start <= 2) &&
          p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
-         (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 &&
+         (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 && p->ramp_sweeps >= 0 &&
          (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&
          (p->momentum == IB3D_MOMENTUM_EULER || p->momentum == IB3D_MOMENTUM_AB2);
 }

@@ -518,8 +518,14 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       for (int q = 0; q < batch; ++q) {
         // the solve's first sweeps at relaxation 1 (smooth_sweeps): Gauss-Seidel damps the
         // high-frequency error that the over-relaxed sweeps barely touch
+        // and then ramp_sweeps sweeps whose relaxation rises linearly from 1 to omega_inner
         const bool smooth = outer == 0 && q < P.smooth_sweeps;
-        const float w = smooth ? 1.0f : om, w1 = smooth ? 0.0f : om1;
+        float w = smooth ? 1.0f : om, w1 = smooth ? 0.0f : om1;
+        if (outer == 0 && q >= P.smooth_sweeps && q < P.smooth_sweeps + P.ramp_sweeps) {
+          const double wr = 1.0 + (double)(q - P.smooth_sweeps + 1) / (P.ramp_sweeps + 1) * (wi - 1.0);
+          w = (float)wr;
+          w1 = (float)(1.0 - wr);
+        }
         if (packed) {
           launch_sor32_packed(c, 0, w, w1);
           launch_sor32_packed(c, 1, w, w1);

@@ -100,6 +100,8 @@ typedef struct ib3d_params {
                              high-frequency part of the initial error by only |omega - 1| per sweep;
                              a few Gauss-Seidel sweeps remove what a coarse-grid guess (the learned
                              warm start) or the new right-hand side adds there. 0: none */
+  int32_t ramp_sweeps;    /* FP32 form only: after the smoothing sweeps, the first pass raises the
+                             relaxation linearly from 1 to omega_inner over this many sweeps. 0: none */
 } ib3d_params;
 
 /* Per-call statistics of the pressure solve (subPcorVcor.f90:60-65 logs the same). */

@@ -40,10 +40,10 @@ def test_python_mirror_binds_every_symbol(ib3d, built_lib):
 def test_params_struct_layout(ib3d, built_lib):
     p = ib3d.default_params()
     # 4 doubles, int64, 6 int32, double, 3 int32 + 4 bytes of tail padding
-    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8 + 4 * 4
+    assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8 + 5 * 4 + 4   # padded to 8 bytes
     assert ib3d.Params.omega_inner.offset == 64 and ib3d.Params.inner_schedule.offset == 72
     assert ib3d.Params.outlet.offset == 76 and ib3d.Params.momentum.offset == 80
-    assert ib3d.Params.smooth_sweeps.offset == 84
+    assert ib3d.Params.smooth_sweeps.offset == 84 and ib3d.Params.ramp_sweeps.offset == 88
     assert ctypes.sizeof(ib3d.SolveStats) == 7 * 8
     assert p.omega == 1.99 and p.eps == 1e-5 and p.criterion == ib3d.CRIT_UPDATE
     assert p.inner_schedule == ib3d.INNER_FIXED
