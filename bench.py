@@ -129,17 +129,20 @@ def load_net(pkg, name: str = "", coarsen: int = 4):
 
 
 def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200.0, 250.0, 300.0, 350.0),
-              steps: int = 24, patches: int = 8) -> dict:
+              steps: int = 24, patches: int = 8, init: str = "", lr0: float = 1e-3) -> dict:
     """Generates snapshots (perturbed runs at the given Reynolds numbers -- by default
     Re 200/250/300/350 --, `steps` steps each, `patches` random patches of 128^3 cells
     per step from step 3), trains with Adam for `seconds` (batch 8, lr 1e-3 then 2e-4
     for the last 30 %), writes the FP32 weights, and compares sweeps on a held-out Re
     275 run (adaptive pass lengths, so that the counts resolve differences below 256
-    sweeps)."""
+    sweeps). With `init` the training starts from those weights (a networks.json name or
+    a path), at learning rate lr0 (then lr0/5 for the last 30 %)."""
     import dataclasses
     import numpy as np
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
-    net = pkg.Net(seed=0)
+    net = load_net(pkg, init, coarsen) if init else None
+    if net is None:
+        net = pkg.Net(seed=0)
     net.set_coarsening(coarsen)
     net.reserve(128 // coarsen, len(reynolds) * (steps - 2) * patches)     # patches of 128^3 cells
     net.coarsen = coarsen
@@ -148,7 +151,7 @@ def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200
     before = fit()
     t0, steps = time.perf_counter(), 0
     while time.perf_counter() - t0 < seconds:
-        lr = 1e-3 if time.perf_counter() - t0 < 0.7 * seconds else 2e-4
+        lr = lr0 if time.perf_counter() - t0 < 0.7 * seconds else lr0 / 5
         learned.train(net, 100, batch=8, lr=lr, chunk=100, seed=steps)
         steps += 100
     after = fit()
@@ -538,6 +541,8 @@ def main():
     ap.add_argument("--train-re", default="200,250,300,350", help="Reynolds numbers of --train-net's runs")
     ap.add_argument("--train-steps", type=int, default=24, help="steps of each --train-net run")
     ap.add_argument("--train-patches", type=int, default=8, help="patches captured per step by --train-net")
+    ap.add_argument("--train-init", default="", help="weights --train-net starts from (default: random)")
+    ap.add_argument("--train-lr", type=float, default=1e-3, help="--train-net's learning rate (then a fifth)")
     ap.add_argument("--weights", default="", help="weights file in ib3d-gpu_gb300/weights (default: networks.json's)")
     ap.add_argument("--moving", action="store_true",
                     help="instead of the step benchmark: the transversely oscillating sphere "
@@ -561,7 +566,8 @@ def main():
         if dist.rank == 0:
             print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds,
                                        args.coarsen, [float(r) for r in args.train_re.split(",")],
-                                       args.train_steps, args.train_patches)), flush=True)
+                                       args.train_steps, args.train_patches, args.train_init,
+                                       args.train_lr)), flush=True)
         dist.close()
         return
     if args.train_moving:
