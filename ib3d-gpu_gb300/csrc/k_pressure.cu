@@ -516,9 +516,9 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       PhaseScope ps(c, PH_SOR32);
       c->launches += 2 * batch;
       for (int q = 0; q < batch; ++q) {
-        // the solve's first sweeps at relaxation 1 (smooth_sweeps): Gauss-Seidel damps the
-        // high-frequency error that the over-relaxed sweeps barely touch
-        // and then ramp_sweeps sweeps whose relaxation rises linearly from 1 to omega_inner
+        // the solve's first sweeps run at relaxation 1 (smooth_sweeps: Gauss-Seidel damps the
+        // high-frequency error that the over-relaxed sweeps barely touch), the next
+        // ramp_sweeps with the relaxation rising linearly from 1 to omega_inner
         const bool smooth = outer == 0 && q < P.smooth_sweeps;
         float w = smooth ? 1.0f : om, w1 = smooth ? 0.0f : om1;
         if (outer == 0 && q >= P.smooth_sweeps && q < P.smooth_sweeps + P.ramp_sweeps) {
