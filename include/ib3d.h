@@ -284,7 +284,7 @@ int ib3d_read_result_text(ib3d_ctx* ctx, const char* path, double* totime, int64
 
 /* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A 3-level 3-D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
- * activations, FP32 accumulation), applied to the domain coarsened 2x2x2 (see
+ * activations, FP32 accumulation), applied to the coarsened domain (see
  * ib3d_net_set_coarsening), predicts the change of the pressure correction
  * from one step to the next, pc^n - pc^{n-1}, from four inputs per cell: the
  * previous correction (p^{n-1} - p^{n-2}), b/dt, p^{n-1}, and the FP64 residual of
@@ -313,11 +313,12 @@ int ib3d_net_dataset_reserve(ib3d_net* net, int S, int64_t capacity);
 int64_t ib3d_net_dataset_size(const ib3d_net* net);
 int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
 /* The network sees the domain coarsened by f = 1, 2 or 4 (default 2): each voxel holds
- * the average of the f^3 cells it covers, and the prediction is taken back to every
- * cell of its voxel -- a learned coarse-grid correction of the smooth error that
- * red-black SOR removes slowest, at 1/f^3 of the inference cost. Capture (S^3
- * voxels = (fS)^3 cells per patch) and inference use the same f; changing it
- * clears the training set. */
+ * the average of the f^3 cells it covers, and the prediction is taken back to the
+ * cells by trilinear interpolation between voxel centres -- a learned coarse-grid
+ * correction of the smooth error that red-black SOR removes slowest, at 1/f^3 of the
+ * inference cost (ib3d_params.smooth_sweeps removes the rough error the
+ * interpolation leaves). Capture (S^3 voxels = (fS)^3 cells per patch) and
+ * inference use the same f; changing it clears the training set. */
 int ib3d_net_set_coarsening(ib3d_net* net, int f);
 int ib3d_net_train(ib3d_net* net, int steps, int batch, double lr, uint64_t seed, double* last_loss);
 /* Keeps the two previous pressures and the previous correction's residual in ctx
