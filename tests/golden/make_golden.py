@@ -12,8 +12,9 @@ Each fixture stores its inputs and the oracle's outputs (see fixtures.py):
                     residual 1e-8
   sphere96_fp64     96x64x64 sphere, Re 100, dt 0.005, omega 1.8, eps 1e-6: 200 FP64 steps
                     (sweeps and drag/lift of every step; fields after steps 1 and 200)
+  sphere96_convective  the same with the convective (Orlanski) outlet
 
-The sphere96 record takes about half an hour on 8 cores; the others a few seconds.
+Each sphere96 record takes about half an hour on 8 cores; the others a few seconds.
 """
 from __future__ import annotations
 
@@ -139,8 +140,19 @@ def make_sphere96_fp64() -> dict:
     return fx
 
 
+def make_sphere96_convective() -> dict:
+    cs = _grids().case("sphere96")
+    fx = _inputs(cs)
+    o = fixtures.build_oracle(_oracle(), fx, outlet=1)
+    fx["counts"] = _counts(o.counts)
+    _steps(o, cs.steps, fx, record_after=(1, cs.steps))
+    o.close()
+    return fx
+
+
 MAKERS = {"tiny_fp64": make_tiny_fp64, "tiny_outlet_ab2": make_tiny_outlet_ab2, "tiny_moving": make_tiny_moving,
-          "poisson24": make_poisson24, "sphere96_fp64": make_sphere96_fp64}
+          "poisson24": make_poisson24, "sphere96_fp64": make_sphere96_fp64,
+          "sphere96_convective": make_sphere96_convective}
 
 
 def main(names) -> None:
