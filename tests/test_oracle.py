@@ -223,3 +223,25 @@ def test_calculate_uc_and_ab2_known_answers(oracle_mod, grids):
     ut_euler = p.get_field("ut")
     p.ns_momentum_ab()                       # resi now holds this state's resid
     assert np.allclose(p.get_field("ut"), ut_euler, rtol=0, atol=1e-13)
+
+
+def test_force_driven_motion_known_answers(oracle_mod, grids):
+    """or_move_body_free (shiftSurfaceNodesMovingbody's force integration): a body of
+    volume pi/6 (D = 1, unit density) at rest under a force F reaches v = F/vol * dt
+    after one step and has moved v * dt; with no force it keeps its velocity; the
+    surface centroids move by exactly the displacements."""
+    import math
+    cs = grids.case("tiny")
+    o = oracle_mod.setup_case(cs)
+    vol = math.pi / 6.0
+    c0 = o.surface()[:3].copy()          # element centroids before the move
+    f = (0.0, 2.0, -1.0)
+    v1 = o.move_body_free(*f)
+    assert np.allclose(v1, [fq / vol * cs.dt for fq in f], rtol=1e-15, atol=0.0)
+    c1 = o.surface()[:3].copy()
+    assert np.allclose(c1 - c0, (v1 * cs.dt)[:, None], rtol=0.0, atol=1e-15)
+    v2 = o.move_body_free(0.0, 0.0, 0.0)
+    assert np.array_equal(v2, v1)
+    c2 = o.surface()[:3].copy()
+    assert np.allclose(c2 - c1, (v2 * cs.dt)[:, None], rtol=0.0, atol=1e-15)
+    o.close()
