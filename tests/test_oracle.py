@@ -245,3 +245,37 @@ def test_force_driven_motion_known_answers(oracle_mod, grids):
     c2 = o.surface()[:3].copy()
     assert np.allclose(c2 - c1, (v2 * cs.dt)[:, None], rtol=0.0, atol=1e-15)
     o.close()
+
+
+def _cell_centres(nodes):
+    c = 0.5 * (nodes[:-1] + nodes[1:])
+    return np.concatenate([[2 * nodes[0] - c[0]], c, [2 * nodes[-1] - c[-1]]])
+
+
+def test_drag_known_answers(oracle_mod, grids):
+    """stressCal1 on fields with exact answers. A uniform stream with p = 0 exerts no
+    force. A linear pressure p = x (fluid at rest) pushes the sphere with
+    -grad(p) * volume = (-pi/6, 0, 0), i.e. Cd_p = 2 F_x / (pi/4) = -4/3, and p = y
+    gives the same lift; the surface pressure is extrapolated from probe points, so
+    the coefficient converges to -4/3 at first order in the core spacing h:
+    (Cd + 4/3) / h is the same on h = 1/8 and 1/16, and the Richardson value
+    2 Cd(1/16) - Cd(1/8) is -4/3 within 0.5 %."""
+    cds = {}
+    for name, h in (("tiny", 1.0 / 8), ("sphere96", 1.0 / 16)):
+        cs = grids.case(name)
+        o = oracle_mod.setup_case(cs)
+        assert np.array_equal(o.stress(True), np.zeros(4))          # u = 1, p = 0
+        shape = o.get_field("p").shape
+        for f in ("u", "v", "w"):
+            o.set_field(f, np.zeros(shape))
+        o.set_field("p", np.broadcast_to(_cell_centres(cs.x)[:, None, None], shape).copy())
+        cx = o.stress(True)
+        o.set_field("p", np.broadcast_to(_cell_centres(cs.y)[None, :, None], shape).copy())
+        cy = o.stress(True)
+        o.close()
+        assert cx[0] == 0.0 and cx[2] == 0.0 and abs(cx[3]) < 1e-12      # no viscous part, no lift
+        assert abs(cy[3] - cx[1]) < 1e-12 and abs(cy[1]) < 1e-12          # p = y: the same, as lift
+        cds[h] = cx[1]
+    e8, e16 = (cds[1 / 8] + 4 / 3) * 8, (cds[1 / 16] + 4 / 3) * 16
+    assert abs(e8 - e16) < 0.02 * abs(e16), (cds, e8, e16)
+    assert abs((2 * cds[1 / 16] - cds[1 / 8]) + 4 / 3) < 0.005 * 4 / 3, cds
