@@ -279,3 +279,30 @@ def test_drag_known_answers(oracle_mod, grids):
     e8, e16 = (cds[1 / 8] + 4 / 3) * 8, (cds[1 / 16] + 4 / 3) * 16
     assert abs(e8 - e16) < 0.02 * abs(e16), (cds, e8, e16)
     assert abs((2 * cds[1 / 16] - cds[1 / 8]) + 4 / 3) < 0.005 * 4 / 3, cds
+
+
+def test_linear_fields_known_answers(oracle_mod, grids):
+    """On the stretched grid of the tiny case, without a body: the divergence
+    (computeDiv) of the face velocity ut = x is exactly 1 in every interior cell, and
+    the shear flow u = y (v = w = p = 0) is steady under the momentum predictor --
+    convection vanishes with v = 0 and the non-uniform second difference of a linear
+    profile is zero -- away from the ghost layers."""
+    cs = grids.case("tiny")
+    o = oracle_mod.Oracle(cs.x, cs.y, cs.z, cs.re, cs.dt, max_sweeps=1)
+    o.no_body()
+    shape = o.get_field("u").shape
+    zero = np.zeros(shape)
+    xf = np.asarray(cs.x)[np.minimum(np.arange(shape[0]), len(cs.x) - 1)]   # ut(i) sits on face x(i)
+    faces = np.broadcast_to(xf[:, None, None], shape).copy()
+    for f, val in (("u", faces), ("v", zero), ("w", zero), ("ut", faces), ("vt", zero), ("wt", zero)):
+        o.set_field(f, val)
+    o.poisson_solver(allow_noconv=True)
+    assert np.array_equal(o.get_field("b")[2:-2, 2:-2, 2:-2], np.ones((shape[0] - 4, shape[1] - 4, shape[2] - 4)))
+    shear = np.broadcast_to(_cell_centres(cs.y)[None, :, None], shape).copy()
+    for f, val in (("u", shear), ("v", zero), ("w", zero), ("p", zero)):
+        o.set_field(f, val)
+    o.ns_momentum()
+    ut = o.get_field("ut")
+    inner = np.s_[4:-4, 4:-4, 4:-4]
+    assert np.max(np.abs(ut[inner] - shear[inner])) < 1e-12 * np.max(np.abs(shear))
+    o.close()
