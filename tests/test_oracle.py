@@ -306,3 +306,20 @@ def test_linear_fields_known_answers(oracle_mod, grids):
     inner = np.s_[4:-4, 4:-4, 4:-4]
     assert np.max(np.abs(ut[inner] - shear[inner])) < 1e-12 * np.max(np.abs(shear))
     o.close()
+
+
+def test_poisson_boundary_rows_on_a_uniform_grid(oracle_mod):
+    """coefficientMatrix's boundary folding (subCoefficientMatrix.f90:36-53) on a
+    uniform grid of spacing h: interior rows (1, -2, 1)/h^2; the inlet and the y, z
+    faces are Neumann (A2 += A1: (0, -1, 1)/h^2 at the first row, (1, -1, 0)/h^2 at
+    the last y and z rows); the outlet is Dirichlet (A2 -= A3: (1, -3, 0)/h^2)."""
+    h = 0.5
+    o = _uniform_oracle(oracle_mod, n=12, h=h)
+    r = 1.0 / (h * h)
+    ax, ay, az = o.acoef(0), o.acoef(1), o.acoef(2)
+    for A in (ax, ay, az):
+        assert np.allclose(A[1:-1], [r, -2 * r, r], rtol=1e-15, atol=0.0)
+        assert np.allclose(A[0], [0.0, -r, r], rtol=1e-15, atol=0.0)
+    assert np.allclose(ax[-1], [r, -3 * r, 0.0], rtol=1e-15, atol=0.0)
+    for A in (ay, az):
+        assert np.allclose(A[-1], [r, -r, 0.0], rtol=1e-15, atol=0.0)
