@@ -272,7 +272,7 @@ int ib3d_synchronize(ib3d_ctx* ctx);
  * reads them back and sets ut = u, vt = v, wt = w. ib3d_write_restart and
  * ib3d_read_restart do the same straight from and into device memory in a binary
  * file (64-byte header "IB3DRST1", nx, ny, nz, totime, ita, ita1, nfields = 4, then
- * u, v, w, p in the Fortran layout), so the driver no longer needs the per-step
+ * u, v, w, p in the Fortran layout), so the Fortran driver no longer needs the per-step
  * download of main.f90:55 to keep a restart. The text pair reads and writes the
  * reference's own `result` file (one "u v w p totime ita ita1" record per cell, k
  * outer), for runs that move between the two codes. A file for another grid size

@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (liboracle.so, built by oracle/build.py).
 
-Test infrastructure only: the checker for the CUDA library and the timed CPU
-baseline of bench.py. Parity status: unpinned by the reference itself (no
+Test infrastructure only: what the CUDA library is tested against, and the timed
+CPU baseline of bench.py. Parity status: unpinned by the reference itself (no
 Fortran compiler, no reference tests or fixtures); pinned by analytic
 known-answer tests and by the committed fixtures in tests/golden/.
 

@@ -77,8 +77,8 @@ def test_poisson_cube_meets_the_record_bit_for_bit(ib3d):
 
 @pytest.mark.parametrize("name,kw", [("sphere96_fp64", {}), ("sphere96_convective", dict(outlet=1))])
 def test_200_steps_of_the_96_case_meet_the_fp64_parity_bar(ib3d, name, kw):
-    """configs[0] as stated: 200 steps, with the reference's active zero-gradient
-    outlet and with the convective (Orlanski) outlet."""
+    """The 96x64x64 sphere at Re 100 for 200 steps, with the reference's active
+    zero-gradient outlet and with the convective (Orlanski) outlet."""
     fx = fixtures.load(name)
     s = fixtures.build_solver(ib3d, fx, **kw)
     assert _counts(s.counts) == fx["counts"].tolist()
