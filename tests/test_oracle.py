@@ -323,3 +323,25 @@ def test_poisson_boundary_rows_on_a_uniform_grid(oracle_mod):
     assert np.allclose(ax[-1], [r, -3 * r, 0.0], rtol=1e-15, atol=0.0)
     for A in (ay, az):
         assert np.allclose(A[-1], [r, -r, 0.0], rtol=1e-15, atol=0.0)
+
+
+def test_normal_distances_follow_the_sphere(oracle_mod, grids):
+    """computeNormDistance (subSearch.f90:599-678): for every IB cell of the 64x48x48
+    case, the signed distance of the pressure node to the plane of its nearest
+    element is the distance to the sphere r - 0.5 up to the faceting of the
+    icosphere (< 1e-3), and those of the six face-centred velocity nodes (u at x -/+
+    h/2, then v, w) are within 5e-3 (the plane of the cell's element, seen from a
+    node half a cell away)."""
+    cs = grids.case("small")
+    o = oracle_mod.setup_case(cs)
+    sr = o.get_search()
+    ib, nd = sr["ib"], sr["normdis"]
+    xc, yc, zc = (_cell_centres(np.asarray(a)) for a in (cs.x, cs.y, cs.z))
+    a, b, c = ib[:, 0] - 1, ib[:, 1] - 1, ib[:, 2] - 1
+    X, Y, Z = xc[a], yc[b], zc[c]
+    x, y, z = (np.asarray(v) for v in (cs.x, cs.y, cs.z))
+    nodes = [(X, Y, Z), (x[a - 1], Y, Z), (x[a], Y, Z), (X, y[b - 1], Z), (X, y[b], Z), (X, Y, z[c - 1]), (X, Y, z[c])]
+    for q, (px, py, pz) in enumerate(nodes):
+        err = np.abs(nd[:, q] - (np.sqrt(px * px + py * py + pz * pz) - 0.5)).max()
+        assert err < (1e-3 if q == 0 else 5e-3), (q, err)
+    o.close()
