@@ -345,3 +345,33 @@ def test_normal_distances_follow_the_sphere(oracle_mod, grids):
         err = np.abs(nd[:, q] - (np.sqrt(px * px + py * py + pz * pz) - 0.5)).max()
         assert err < (1e-3 if q == 0 else 5e-3), (q, err)
     o.close()
+
+
+def test_tagging_follows_the_sphere(oracle_mod, grids):
+    """tagging (subSearch.f90:134-321) against the exact sphere on the 64x48x48 case:
+    every cell whose eight corners lie inside r < 0.5 - 2e-3 is solid, every cell
+    whose corners all lie outside r > 0.5 + 2e-3 is fluid, and the IB cells are all
+    among the cells the surface cuts (the 2e-3 band covers the icosphere's
+    faceting)."""
+    cs = grids.case("small")
+    o = oracle_mod.setup_case(cs)
+    cell = o.get_search()["cell"]
+    o.close()
+    x, y, z = (np.asarray(v) for v in (cs.x, cs.y, cs.z))
+    nx, ny, nz = len(x) - 1, len(y) - 1, len(z) - 1
+    rmin = np.full((nx, ny, nz), np.inf)
+    rmax = np.zeros((nx, ny, nz))
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                X = x[dx:nx + dx][:, None, None]
+                Y = y[dy:ny + dy][None, :, None]
+                Z = z[dz:nz + dz][None, None, :]
+                r = np.sqrt(X * X + Y * Y + Z * Z)
+                rmin, rmax = np.minimum(rmin, r), np.maximum(rmax, r)
+    flags = cell[1:nx + 1, 1:ny + 1, 1:nz + 1]
+    inside, outside = rmax < 0.5 - 2e-3, rmin > 0.5 + 2e-3
+    assert inside.any() and np.all(flags[inside] == 1)
+    assert np.all(flags[outside] == 0)
+    cut = ~inside & ~outside
+    assert np.all(np.isin(flags[cut], (0, 2))) and np.all(cut[flags == 2])
