@@ -375,3 +375,68 @@ def test_tagging_follows_the_sphere(oracle_mod, grids):
     assert np.all(flags[outside] == 0)
     cut = ~inside & ~outside
     assert np.all(np.isin(flags[cut], (0, 2))) and np.all(cut[flags == 2])
+
+
+def _cube(lo: float, hi: float):
+    """Axis-aligned cube [lo, hi]^3 as 12 outward counter-clockwise triangles (1-based)."""
+    v = np.array([[lo, lo, lo], [hi, lo, lo], [hi, hi, lo], [lo, hi, lo],
+                  [lo, lo, hi], [hi, lo, hi], [hi, hi, hi], [lo, hi, hi]])
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (0, 4, 7, 3)]
+    tris = [t for a, b, c, d in quads for t in ((a, b, c), (a, c, d))]
+    return v, np.array(tris, dtype=np.int64) + 1
+
+
+def test_ghost_point_forcing_reproduces_affine_fields(oracle_mod):
+    """velocityForcing1's quadratic ghost values (subForcing.f90:107-652) are exact for
+    a field that is affine along the wall normal and meets the no-slip condition:
+    a cube [1.02, 1.98]^3 at rest on a uniform grid (h = 0.1), ut = x - 1.98 (zero
+    on the +x face), vt = wt = 0. Every ghost u value near the middle of the +x face,
+    set to 10 beforehand, becomes x - 1.98 within 1e-12, and vt, wt stay 0 there."""
+    h, n, lo, hi = 0.1, 30, 1.02, 1.98
+    x = np.arange(n + 1) * h
+    o = oracle_mod.Oracle(x, x.copy(), x.copy(), re=100.0, deltat=0.01)
+    v, tris = _cube(lo, hi)
+    o.set_mesh(v, tris)
+    o.search((2, n + 1, 2, n + 1, 2, n + 1))
+    shape = o.get_field("u").shape
+    xf = x[np.minimum(np.arange(shape[0]), n)]                 # ut(i) sits on face x(i)
+    yc = (np.arange(shape[1]) - 0.5) * h                       # cell centres in y and z
+    exact = np.broadcast_to((xf - hi)[:, None, None], shape).copy()
+    band = ((xf[:, None, None] > hi - 0.15) & (xf[:, None, None] < hi)
+            & (np.abs(yc[None, :, None] - 1.5) < 0.3) & (np.abs(yc[None, None, :] - 1.5) < 0.3))
+    ut0 = np.where(band, 10.0, exact)
+    zero = np.zeros(shape)
+    for f, val in (("u", ut0), ("ut", ut0), ("v", zero), ("vt", zero), ("w", zero), ("wt", zero)):
+        o.set_field(f, val)
+    o.velocity_forcing()
+    ut, vt, wt = o.get_field("ut"), o.get_field("vt"), o.get_field("wt")
+    ghost = band & (ut != 10.0)
+    assert ghost.sum() > 20, ghost.sum()
+    assert np.max(np.abs(ut[ghost] - exact[ghost])) < 1e-12
+    assert np.max(np.abs(vt[ghost])) < 1e-12 and np.max(np.abs(wt[ghost])) < 1e-12
+    o.close()
+
+
+def test_ghost_point_pressure_forcing_reproduces_fields_with_zero_normal_gradient(oracle_mod):
+    """pressureForcing1 (subForcing.f90:2-103, dp/dn = 0 for a body at rest) is exact
+    for a pressure that does not vary along the wall normal: near the middle of the
+    +x face of the cube, p = y, and every ghost pressure there, set to 10
+    beforehand, becomes its cell's y within 1e-12."""
+    h, n, lo, hi = 0.1, 30, 1.02, 1.98
+    x = np.arange(n + 1) * h
+    o = oracle_mod.Oracle(x, x.copy(), x.copy(), re=100.0, deltat=0.01)
+    v, tris = _cube(lo, hi)
+    o.set_mesh(v, tris)
+    o.search((2, n + 1, 2, n + 1, 2, n + 1))
+    shape = o.get_field("p").shape
+    c = (np.arange(shape[0]) - 0.5) * h                        # cell centres (padded index)
+    exact = np.broadcast_to(c[None, :, None], shape).copy()    # p = y
+    band = ((c[:, None, None] > hi - 0.15) & (c[:, None, None] < hi)
+            & (np.abs(c[None, :, None] - 1.5) < 0.3) & (np.abs(c[None, None, :] - 1.5) < 0.3))
+    o.set_field("p", np.where(band, 10.0, exact))
+    o.pressure_forcing()
+    p = o.get_field("p")
+    ghost = band & (p != 10.0)
+    assert ghost.sum() > 10, ghost.sum()
+    assert np.max(np.abs(p[ghost] - exact[ghost])) < 1e-12
+    o.close()
