@@ -466,3 +466,26 @@ def test_projection_makes_the_velocity_divergence_free(oracle_mod, grids):
     assert np.abs(o.get_field("b")[s]).max() > 1.0
     assert np.abs(div).max() < 1e-12, np.abs(div).max()
     o.close()
+
+
+def test_third_order_upwind_is_exact_for_cubics_on_a_stretched_grid(oracle_mod, grids):
+    """non_uni_coeff's own-axis family (subNavierStokes.f90:36-116) on a stretched
+    axis: the five-point convection stencil, divided by its sixth coefficient and
+    the spacing, is the first derivative of any cubic exactly at every node it is
+    used for -- third order on non-uniform spacing -- and its dissipation stencil
+    annihilates cubics where the spacing is uniform."""
+    nodes, _, _ = grids.stretched_axis(-2.0, 3.0, 20, -0.5, 0.5, 0.125)
+    o = oracle_mod.Oracle(nodes, nodes.copy(), nodes.copy(), re=100.0, deltat=0.01)
+    c = [o.conv_coef(0, m) for m in range(12)]
+    f = lambda x: 0.3 * x ** 3 - x ** 2 + 2.0 * x + 1.0
+    df = lambda x: 0.9 * x ** 2 - 2.0 * x + 2.0
+    for i in range(4, o.nx):
+        xs = [nodes[i + 1], nodes[i], nodes[i - 1], nodes[i - 2], nodes[i - 3]]   # u(i+2) .. u(i-2)
+        sa = sum(c[m][i] * f(xs[m]) for m in range(5))
+        expect = c[5][i] * (nodes[i] - nodes[i - 1]) * df(nodes[i - 1])
+        assert abs(sa - expect) <= 1e-11 * abs(expect), (i, sa, expect)
+        h = np.diff(nodes[i - 3:i + 2])
+        if np.all(h == h[0]):
+            sk = sum(c[6 + m][i] * f(xs[m]) for m in range(5))
+            assert abs(sk) <= 1e-13 * max(abs(c[6 + m][i] * f(xs[m])) for m in range(5)), (i, sk)
+    o.close()
