@@ -488,4 +488,14 @@ def test_third_order_upwind_is_exact_for_cubics_on_a_stretched_grid(oracle_mod, 
         if np.all(h == h[0]):
             sk = sum(c[6 + m][i] * f(xs[m]) for m in range(5))
             assert abs(sk) <= 1e-13 * max(abs(c[6 + m][i] * f(xs[m])) for m in range(5)), (i, sk)
+    # the transverse families (a velocity carried across the other axes, at cell
+    # centres): exact for cubics with the centre-to-centre spacing as normaliser
+    centres = 0.5 * (nodes[:-1] + nodes[1:])
+    for fam in (3, 4, 5):
+        c = [o.conv_coef(fam, m) for m in range(6)]
+        for i in range(4, o.nx - 1):
+            xs = [centres[i], centres[i - 1], centres[i - 2], centres[i - 3], centres[i - 4]]
+            sa = sum(c[m][i] * f(xs[m]) for m in range(5))
+            expect = c[5][i] * (centres[i - 1] - centres[i - 2]) * df(centres[i - 2])
+            assert abs(sa - expect) <= 1e-11 * abs(expect), (fam, i, sa, expect)
     o.close()
