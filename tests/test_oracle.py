@@ -499,3 +499,22 @@ def test_third_order_upwind_is_exact_for_cubics_on_a_stretched_grid(oracle_mod, 
             expect = c[5][i] * (centres[i - 1] - centres[i - 2]) * df(centres[i - 2])
             assert abs(sa - expect) <= 1e-11 * abs(expect), (fam, i, sa, expect)
     o.close()
+
+
+def test_diffusion_is_exact_for_a_quadratic_profile(oracle_mod, grids):
+    """nsMomentum's viscous term (subNavierStokes.f90:879-887) on the stretched grid of
+    the tiny case: for u = y^2 with v = w = p = 0 the convection vanishes and the
+    non-uniform three-point second difference is exact, so ut = u + dt * 2 / Re away
+    from the ghost layers."""
+    cs = grids.case("tiny")
+    o = oracle_mod.Oracle(cs.x, cs.y, cs.z, cs.re, cs.dt)
+    o.no_body()
+    shape = o.get_field("u").shape
+    u = np.broadcast_to((_cell_centres(np.asarray(cs.y)) ** 2)[None, :, None], shape).copy()
+    zero = np.zeros(shape)
+    for f, val in (("u", u), ("v", zero), ("w", zero), ("p", zero)):
+        o.set_field(f, val)
+    o.ns_momentum()
+    rate = (o.get_field("ut") - u)[4:-4, 4:-4, 4:-4] / cs.dt * cs.re
+    assert np.max(np.abs(rate - 2.0)) < 1e-9
+    o.close()
