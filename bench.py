@@ -1,13 +1,16 @@
 #!/usr/bin/env python
 """Benchmark of the IB3D per-time-step hot path on one GB300.
 
-Workload (sphere256): flow past a fixed sphere (icosphere D = 1, 2562 nodes,
-5120 triangles) at Re 300 on a 256x192x192 non-uniform staggered grid
-(D/40 uniform core on [-0.8,0.8]^3, geometric stretching to the domain
-[-5,15]x[-5,5]x[-5,5]), dt = 0.002, impulsive start u = 1. Each step is the
-reference's full step (momentum predictor, boundary conditions, ghost-point
-forcing, red-black SOR pressure solve with relaxation 1.99 to an FP64 residual
-L-inf <= 1e-6, pressure/velocity correction, drag/lift).
+Workload (sphere256, Re 275): flow past a fixed sphere (icosphere D = 1, 2562
+nodes, 5120 triangles) on a 256x192x192 non-uniform staggered grid (D/40
+uniform core on [-0.8,0.8]^3, geometric stretching to the domain
+[-5,15]x[-5,5]x[-5,5]), dt = 0.002, impulsive start u = 1, at Re 275 -- the
+Reynolds number the shipped network was never trained on (its training runs used
+200-350 without 275). Each step is the reference's full step (momentum predictor,
+boundary conditions, ghost-point forcing, red-black SOR pressure solve with
+relaxation 1.99 to an FP64 residual L-inf <= 1e-6, pressure/velocity correction,
+drag/lift). Every arm runs W untimed warm-up steps from the impulsive start and
+times steps W+1..W+K: the same physical steps in every arm.
 
 value  = steps/s of the headline form: FP32 red-black sweeps inside an FP64
          defect-correction loop (passes of 512 sweeps, the last one cut to what
@@ -16,15 +19,19 @@ value  = steps/s of the headline form: FP32 red-black sweeps inside an FP64
          residual as the plain path. `fp32_previous_correction` is the same form
          warm-started from the previous step's correction (the network's
          fallback).
-plain  = steps/s of the plain FP64 path (reference arithmetic, zero initial
-         correction) over the same physical steps.
+plain_fp64 / plain_fp64_fast = steps/s of the plain FP64 method (zero initial
+         correction, FP64 sweeps): reference arithmetic (bit-identical to the
+         oracle), and the fast form (contracted multiply-adds, omega/diag per
+         cell). `drag_rel_vs_fp64` / `lift_rel_vs_fp64`: the headline's worst
+         per-step error against the reference-arithmetic path.
 e2e    = the headline form through the C ABI with host buffers: the state is
          uploaded from pinned host memory at the start of the timed region and
          every step downloads u,v,w,ut,vt,wt,p to pinned host memory, as the
          reference's per-step `update host` (main.f90:55) does.
-cpu_baseline / --impl reference = the FP64 oracle (the reference's algorithm
-         restated in C, OpenMP on all host cores), timed on a bounded sample
-         and scaled to steps/s (see `sample`).
+cpu_baseline = the FP64 oracle (the reference's algorithm restated in C, OpenMP
+         on all host cores) on a bounded sample (two capped steps) scaled to the
+         plain path's sweep count on the same window. --impl reference times whole
+         oracle steps of the same window instead.
 
 Timing: W untimed warm-up steps, then K steps between CUDA events recorded on
 the library's own stream, with a barrier and synchronize on both sides; every
@@ -46,24 +53,18 @@ import time
 
 ROOT = pathlib.Path(__file__).resolve().parent
 METRIC = "steps/s at 256×192×192 sphere: learned+FP32 vs plain FP64, residual ≤1e-6"
-# Algorithmic bytes of one colour pass of the colour-packed FP32 sweep (one k_sor32p
-# launch), per grid cell: the updated colour's r (4 B) and e (4 B read, 4 B written)
-# over half the cells, and the other colour's e (4 B) over the other half.
-BYTES_SOR32_LAUNCH = 8.0
-# DRAM bytes (read + written) per k_sor32p launch on the 256x192x192 workload from
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_sor32p_sphere256.md).
-# Warm: inside the sweep loop, caches as the previous pass left them (mean of four
-# launches, 22,946,560 B) -- the arrays stay in L2. Cold: caches flushed before the
-# launch (mean of a red and a black launch). Other workloads scale them by their cell
-# count.
-DRAM_BYTES_PER_CELL_SOR32 = 22946560.0 / 4 / 9437184.0
-DRAM_BYTES_PER_CELL_SOR32_COLD = 60741760.0 / 9437184.0
-BYTES_SOR64 = 25.0   # FP64 sweep: pc 8 r + b 8 + pc 8 w + flag 1
-
-
-def traffic_per_launch(cs, cold: bool = False) -> float:
-    """Measured DRAM bytes of one k_sor32p launch on this workload (warm L2 unless cold)."""
-    return (DRAM_BYTES_PER_CELL_SOR32_COLD if cold else DRAM_BYTES_PER_CELL_SOR32) * cs.cells
+# the Reynolds number of the headline run: held out of every training set of the shipped networks
+HEADLINE_RE = 275.0
+# Algorithmic bytes per grid cell of one red+black sweep: FP32 inner sweep = e read 4 + e
+# written 4 + r 4 + flag 1; FP64 sweep = pc read 8 + written 8 + b/dt 8 + flag 1.
+BYTES_SOR32_SWEEP = 13.0
+BYTES_SOR64_SWEEP = 25.0
+# DRAM bytes (read + written) per grid cell and sweep of the FP32 sweep kernel at
+# 256x192x192, from one ncu capture of the launches inside the sweep loop (warm: caches as
+# the previous launch left them) and of a launch after a cache flush (cold). Other
+# workloads scale them by their cell count.
+DRAM_BYTES_PER_CELL_SWEEP32 = 2 * 22946560.0 / 4 / 9437184.0
+DRAM_BYTES_PER_CELL_SWEEP32_COLD = 2 * 60741760.0 / 9437184.0
 
 
 def package():
@@ -78,10 +79,12 @@ def package():
     return mod
 
 
-def workload(pkg, name: str):
+def workload(pkg, name: str, re: float | None = None):
     cs = pkg.grids.case(name)
     cs.omega = 1.99     # the reference's relaxation factor (subPcorVcor.f90:158)
     cs.eps = 1e-6
+    if re is not None:
+        cs.re = float(re)
     return cs
 
 
@@ -95,12 +98,13 @@ def workload(pkg, name: str):
 # the previous correction; 4-12 less, 64-256 worse)
 FAST = dict(precision=1, warm_start=1, criterion=1, inner_sweeps=512, inner_schedule=2, omega_inner=1.9937,
             smooth_sweeps=6, ramp_sweeps=32, sweep_kernel=0, max_sweeps=400000)
+# the plain FP64 method: zero initial correction, FP64 sweeps, residual tested every 8 sweeps;
+# reference arithmetic, and the fast form (IB3D_PREC_FP64_FAST)
 PLAIN = dict(precision=0, warm_start=0, criterion=1, check_every=8, max_sweeps=400000)
-SWEEP_TABLE = ROOT / "oracle" / "sweeps_sphere256.json"
+PLAIN_FAST = dict(PLAIN, precision=2)
 # U-Net weights trained on the GPU by this library's own kernels (bench.py --train-net);
 # networks.json names the default and each file's coarsening
 WEIGHTS_DIR = ROOT / "ib3d-gpu_gb300" / "weights"
-
 
 def load_net(pkg, name: str = "", coarsen: int = 4):
     """The trained warm-start network (networks.json's default, or `name` there), or
@@ -273,14 +277,22 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+
+
 # -------------------------------------------------------------- GPU arms
 
 def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bool = True, clocks=None,
-            net=None):
+            net=None, restart: str | None = None):
+    """W untimed warm-up steps, then K steps timed with CUDA events on the library's
+    stream; returns the time, every timed step's solve statistics and drag/lift, the
+    phase timers and the clocks. `restart` starts from a restart file (the first step
+    after it runs stressCal1, as a fresh run does)."""
     import torch
     s = pkg.setup_case(cs, **mode)
     if net is not None:
         s.attach_net(net)
+    if restart:
+        s.read_restart(restart)
     first = True
     for _ in range(warmup):
         s.step(first)
@@ -296,11 +308,12 @@ def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bo
         clocks.start()
     torch.cuda.nvtx.range_push("ib3d_timed")
     e0.record(stream)
-    stats, coef = [], None
+    stats, coefs = [], []
     for _ in range(steps):
         st, coef = s.step(first)
         first = False
         stats.append(st)
+        coefs.append([float(c) for c in coef])
     e1.record(stream)
     torch.cuda.nvtx.range_pop()
     e1.synchronize()
@@ -310,15 +323,30 @@ def run_arm(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, timers: bo
     t = e0.elapsed_time(e1) / 1e3
     tm = s.timers_read() if timers else None
     s.close()
-    return {"seconds": t, "stats": stats, "coef": list(map(float, coef)), "timers": tm, "clocks": clk}
+    return {"seconds": t, "stats": stats, "coefs": coefs, "coef": coefs[-1], "timers": tm, "clocks": clk}
 
 
-def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None):
+def coef_errors(coefs, ref_coefs) -> dict:
+    """Worst per-step drag and lift error of one arm against another on the same steps:
+    drag relative to the reference drag, lift relative to the reference lift (floored at
+    1e-3 of the drag, since the lift of a sphere passes through zero)."""
+    cd_err = cl_err = 0.0
+    for c, r in zip(coefs, ref_coefs):
+        cd, cd_ref = c[0] + c[1], r[0] + r[1]
+        cl, cl_ref = c[2] + c[3], r[2] + r[3]
+        cd_err = max(cd_err, abs(cd - cd_ref) / abs(cd_ref))
+        cl_err = max(cl_err, abs(cl - cl_ref) / max(abs(cl_ref), 1e-3 * abs(cd_ref)))
+    return {"drag_rel": cd_err, "lift_rel": cl_err, "steps_compared": min(len(coefs), len(ref_coefs))}
+
+
+def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None, restart: str | None = None):
     """The headline form through the C ABI with pinned host buffers in the timed region."""
     import torch
     s = pkg.setup_case(cs, **mode)
     if net is not None:
         s.attach_net(net)
+    if restart:
+        s.read_restart(restart)
     first = True
     for _ in range(warmup):
         s.step(first)
@@ -351,26 +379,42 @@ def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None):
     return {"seconds": t, "h2d": 4 * n3 * 8 / steps, "d2h": 7 * n3 * 8 + 4 * 8}
 
 
+def spin_up(pkg, cs, nsteps: int, path: str) -> dict:
+    """Runs the headline form (previous-correction warm start) for `nsteps` steps from
+    the impulsive start and writes a restart file: a developed wake to time from."""
+    t0 = time.perf_counter()
+    s = pkg.setup_case(cs, **FAST)
+    sweeps = []
+    for n in range(nsteps):
+        st, _ = s.step(n == 0)
+        sweeps.append(st["sweeps"])
+    s.write_restart(path, totime=nsteps * cs.dt, ita=nsteps, ita1=nsteps)
+    s.close()
+    return {"steps": nsteps, "seconds": time.perf_counter() - t0, "t_end": nsteps * cs.dt,
+            "fp32_sweeps_last_10": sum(sweeps[-10:]) / max(1, len(sweeps[-10:]))}
+
+
 # ---------------------------------------------------------- CPU baseline
 
-def sweep_table() -> list[int]:
-    if SWEEP_TABLE.exists():
-        return json.loads(SWEEP_TABLE.read_text())["sweeps"]
-    return []
-
-
-def cpu_sample(pkg, cs, sweeps_per_step: float, threads: int) -> dict:
-    """Times the FP64 oracle (the reference's algorithm) on two capped steps of the
-    workload and scales to steps/s: t_step = t_fixed + n * t_sweep, where t_sweep
-    and t_fixed come from steps capped at 8 and 24 sweeps, and n is the number of
-    sweeps the full FP64 solve takes per step (the FP64 GPU path is bit-identical to
-    the oracle, so its sweep counts are the oracle's)."""
+def _oracle():
     if str(ROOT) not in sys.path:
         sys.path.insert(0, str(ROOT))
     from oracle import oracle
+    return oracle
+
+
+def cpu_sample(pkg, cs, sweeps_per_step: float, threads: int) -> dict:
+    """Times the FP64 oracle (the reference's algorithm, its sweep loop in the row
+    form) on two capped steps of the workload and scales to steps/s: t_step = t_fixed
+    + n * t_sweep, where t_sweep and t_fixed come from steps capped at 8 and 40 sweeps,
+    and n is the number of sweeps the plain FP64 path took on the timed window (the
+    reference-arithmetic GPU path is bit-identical to the oracle, so its sweep counts
+    are the oracle's)."""
+    oracle = _oracle()
     oracle.set_threads(threads)
     s1, s2 = 8, 40
     o = oracle.setup_case(cs, criterion=1, check_every=8, max_sweeps=1)
+    o.set_sweep_rows(True)
     o.step(True, allow_noconv=True)          # first step: drag-probe search and thread start-up, untimed
     o.set_solver(cs.omega, cs.eps, 1, s1, 8)
     t0 = time.perf_counter()
@@ -386,10 +430,57 @@ def cpu_sample(pkg, cs, sweeps_per_step: float, threads: int) -> dict:
     t_step = t_fixed + sweeps_per_step * t_sweep
     return {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads, "kind": "port",
             "sample": (f"FP64 oracle (C restatement of the reference, OpenMP {threads} threads) on the "
-                       f"{cs.name} workload: after one untimed step, 2 steps capped at {s1} and {s2} SOR sweeps gave "
-                       f"t_sweep={t_sweep * 1e3:.2f} ms and t_fixed={t_fixed:.3f} s per step, scaled to "
-                       f"{sweeps_per_step:.0f} sweeps per step (the FP64 path's count on the same steps)"),
+                       f"{cs.name} Re {cs.re:g} workload: after one untimed step, 2 steps capped at {s1} and {s2} SOR "
+                       f"sweeps gave t_sweep={t_sweep * 1e3:.2f} ms and t_fixed={t_fixed:.3f} s per step, scaled to "
+                       f"{sweeps_per_step:.0f} sweeps per step (the plain FP64 path's count on the timed steps)"),
             "t_sweep_s": t_sweep, "t_fixed_s": t_fixed, "sample_seconds": t1 + t2}
+
+
+def reference_arm(pkg, cs, warmup: int, steps: int, threads: int, budget_s: float) -> dict:
+    """The reference's algorithm on the host cores, whole steps: the FP64 oracle (OpenMP
+    on `threads` threads, the sweep loop in its bit-identical row form) runs the W
+    warm-up steps from the impulsive start untimed, then times steps W+1..W+K one by
+    one, each a complete step to the FP64 residual tolerance. A step that would end
+    past `budget_s` seconds of timed work is not started (the line then reports the
+    steps it timed). Cross-check: a least-squares fit t_step = t_fixed + n t_sweep
+    over the timed steps."""
+    oracle = _oracle()
+    oracle.set_threads(threads)
+    t_setup = time.perf_counter()
+    o = oracle.setup_case(cs, criterion=1, check_every=8, max_sweeps=400000)
+    o.set_sweep_rows(True)
+    t_setup = time.perf_counter() - t_setup
+    first = True
+    tw = time.perf_counter()
+    warm_sweeps = []
+    for _ in range(warmup):
+        st, _ = o.step(first)
+        first = False
+        warm_sweeps.append(st["sweeps"])
+    tw = time.perf_counter() - tw
+    times, sweeps, coefs = [], [], []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        if times and (time.perf_counter() - t0) + max(times) > budget_s:
+            break
+        ta = time.perf_counter()
+        st, coef = o.step(first)
+        first = False
+        times.append(time.perf_counter() - ta)
+        sweeps.append(st["sweeps"])
+        coefs.append([float(c) for c in coef])
+    elapsed = time.perf_counter() - t0
+    o.close()
+    fit = None
+    if len(times) >= 2 and max(sweeps) > min(sweeps):
+        n = len(times)
+        mx, my = sum(sweeps) / n, sum(times) / n
+        sxx = sum((x - mx) ** 2 for x in sweeps)
+        t_sweep = sum((x - mx) * (y - my) for x, y in zip(sweeps, times)) / sxx
+        fit = {"t_sweep_ms": 1e3 * t_sweep, "t_fixed_s": my - t_sweep * mx}
+    return {"value": len(times) / elapsed, "seconds": elapsed, "steps_timed": len(times),
+            "seconds_per_step": times, "sweeps_per_step": sweeps, "coefs": coefs, "warmup_seconds": tw,
+            "warmup_sweeps": warm_sweeps, "setup_seconds": t_setup, "fit": fit, "threads": threads}
 
 
 # ------------------------------------------------------------------ main
@@ -403,6 +494,7 @@ def run_poisson(pkg, n: int) -> dict:
     out = {"workload": f"standalone Poisson {n}^3, tanh-clustered, all-Neumann, omega 1.85, residual 1e-8",
            "cells": n ** 3}
     arms = {"fp64": dict(precision=0, criterion=1, check_every=8),
+            "fp64_fast": dict(precision=2, criterion=1, check_every=8),
             "fp32dc": dict(precision=1, criterion=1, inner_sweeps=256, omega_inner=1.85, sweep_kernel=0)}
     for name, kw in arms.items():
         p = pkg.default_params(re=100.0, deltat=1.0, omega=1.85, eps=1e-8, max_sweeps=1_000_000)
@@ -415,12 +507,12 @@ def run_poisson(pkg, n: int) -> dict:
         st = s.redblack_sor()
         tm = s.timers_read()
         sweeps = st["sweeps"]
-        if name == "fp64":
+        if name != "fp32dc":
             t_sweep = tm["sor64_ms"] / max(tm["sweeps64"], 1) * 1e-3
-            gbs = BYTES_SOR64 * n ** 3 / t_sweep / 1e9
+            gbs = BYTES_SOR64_SWEEP * n ** 3 / t_sweep / 1e9
         else:
             t_sweep = tm["sor32_ms"] / max(tm["sweeps32"], 1) * 1e-3
-            gbs = 2 * BYTES_SOR32_LAUNCH * n ** 3 / t_sweep / 1e9
+            gbs = BYTES_SOR32_SWEEP * n ** 3 / t_sweep / 1e9
         out[name] = {"sweeps": sweeps, "seconds": st["solve_seconds"], "sweeps_per_s": sweeps / st["solve_seconds"],
                      "final_residual": st["final_err"], "ms_per_sweep": t_sweep * 1e3, "sweep_gbs_algorithmic": gbs}
         s.close()
@@ -514,6 +606,47 @@ def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, f
             "drag_lift": list(map(float, coef)), "y_end": y}
 
 
+
+
+def developed_run(pkg, cs, spinup: int, warmup: int, steps: int, dist: Dist, net, arms: set) -> dict:
+    """Every arm timed from the same developed wake: the headline form (previous-
+    correction warm start) spins the impulsive start up for `spinup` steps untimed and
+    writes a restart file; each arm loads it, runs W warm-up steps and times K."""
+    fd, path = tempfile.mkstemp(suffix=".ib3drst")
+    os.close(fd)
+    try:
+        out = {"workload": f"{cs.name} {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]}, Re {cs.re:g}, developed wake: "
+                           f"steps {spinup + warmup + 1}..{spinup + warmup + steps} (t = "
+                           f"{(spinup + warmup + 1) * cs.dt:g}..{(spinup + warmup + steps) * cs.dt:g})",
+               "spin_up": spin_up(pkg, cs, spinup, path)}
+        res = {}
+        if net is not None:
+            res["learned"] = run_arm(pkg, cs, dict(FAST, warm_start=pkg.WARM_LEARNED), warmup, steps, dist, net=net,
+                                     restart=path)
+        res["previous_correction"] = run_arm(pkg, cs, FAST, warmup, steps, dist, restart=path)
+        if "plain_fast" in arms:
+            res["plain_fp64_fast"] = run_arm(pkg, cs, PLAIN_FAST, warmup, steps, dist, restart=path)
+        if "plain" in arms:
+            res["plain_fp64"] = run_arm(pkg, cs, PLAIN, warmup, steps, dist, restart=path)
+        ref = res.get("plain_fp64") or res.get("plain_fp64_fast")
+        for name, r in res.items():
+            out[name] = {"value": steps / r["seconds"], "unit": "steps/s",
+                         "sweeps_per_step": sum(s["sweeps"] for s in r["stats"]) / steps,
+                         "worst_final_residual": max(s["final_err"] for s in r["stats"])}
+            if ref is not None and r is not ref:
+                out[name]["vs_plain"] = coef_errors(r["coefs"], ref["coefs"])
+        if "learned" in res:
+            out["learned_sweeps_saved"] = 1.0 - out["learned"]["sweeps_per_step"] / \
+                out["previous_correction"]["sweeps_per_step"]
+        plains = [out[k]["value"] for k in ("plain_fp64", "plain_fp64_fast") if k in out]
+        head = out.get("learned", out["previous_correction"])["value"]
+        if plains:
+            out["speedup_vs_fastest_plain"] = head / max(plains)
+        return out
+    finally:
+        os.unlink(path)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,11 +654,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--case", default="sphere256")
-    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 arm")
+    ap.add_argument("--re", type=float, default=HEADLINE_RE,
+                    help="Reynolds number of the step benchmark (default 275, held out of the network's training)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--record-sweeps", type=int, default=0,
-                    help="write the FP64 sweep counts of the first N steps to oracle/sweeps_<case>.json")
-    ap.add_argument("--record-out", default=None, help="output path of --record-sweeps")
+    ap.add_argument("--ref-budget", type=float, default=1200.0,
+                    help="--impl reference: seconds of timed CPU steps after which no further step is started")
+    ap.add_argument("--developed", type=int, default=0,
+                    help="instead of the step benchmark: spin the flow up for this many steps, then time every "
+                         "arm from that developed wake")
     ap.add_argument("--poisson", type=int, default=0,
                     help="instead of the step benchmark: the standalone all-Neumann Poisson cube of this edge "
                          "(omega 1.85, residual 1e-8), FP64 and FP32-sweep forms")
@@ -548,13 +684,14 @@ def main():
                     help="instead of the step benchmark: the transversely oscillating sphere "
                          "(y = 0.2 sin(2 pi 0.2 t), search every step) on --case (default sphere384), "
                          "FP32 form and plain FP64")
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of --moving's plain FP64 arm")
     ap.add_argument("--compare-fp64", type=int, default=0,
                     help="instead of the benchmark: this many steps of the FP32 form (learned warm start) "
                          "against the plain FP64 path: drag/lift and field differences")
     ap.add_argument("--set", default="",
                     help="comma-separated key=value overrides of the FP32-sweep arm's solver parameters")
-    ap.add_argument("--arms", default="fast,learned,plain,e2e,cpu",
-                    help="comma-separated subset of fast,learned,plain,e2e,cpu (profiling runs use 'fast')")
+    ap.add_argument("--arms", default="learned,fast,plain_fast,plain,e2e,cpu",
+                    help="comma-separated subset of learned,fast,plain_fast,plain,e2e,cpu")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
     dist = Dist()
@@ -562,6 +699,7 @@ def main():
     for kv in filter(None, args.set.split(",")):
         k, v = kv.split("=")
         FAST[k.strip()] = float(v) if "." in v or "e" in v else int(v)
+    arms = set(args.arms.split(","))
     if args.train_net:
         if dist.rank == 0:
             print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds,
@@ -587,10 +725,10 @@ def main():
             if mnet is not None:
                 out["fp32_learned"] = run_moving(pkg, mcs, FAST, warmup, args.steps, net=mnet)
                 out["fp32_learned"]["weights"] = mnet.weights
-            out["plain_fp64"] = run_moving(pkg, mcs, PLAIN, warmup, max(1, args.plain_steps // 2))
-            out["speedup"] = out["fp32"]["value"] / out["plain_fp64"]["value"]
+            out["plain_fp64_fast"] = run_moving(pkg, mcs, PLAIN_FAST, warmup, max(1, args.plain_steps))
+            out["speedup_vs_plain_fast"] = out["fp32"]["value"] / out["plain_fp64_fast"]["value"]
             if mnet is not None:
-                out["speedup_learned"] = out["fp32_learned"]["value"] / out["plain_fp64"]["value"]
+                out["speedup_learned_vs_plain_fast"] = out["fp32_learned"]["value"] / out["plain_fp64_fast"]["value"]
             print(json.dumps(out), flush=True)
         dist.close()
         return
@@ -601,89 +739,109 @@ def main():
         return
     if args.compare_fp64:
         if dist.rank == 0:
-            print(json.dumps(compare_fp64(pkg, workload(pkg, args.case), args.compare_fp64,
+            print(json.dumps(compare_fp64(pkg, workload(pkg, args.case, args.re), args.compare_fp64,
                                           load_net(pkg, args.weights, args.coarsen))), flush=True)
         dist.close()
         return
-    cs = workload(pkg, args.case)
+    cs = workload(pkg, args.case, args.re)
     threads = os.cpu_count() or 1
+    window = f"steps {warmup + 1}..{warmup + args.steps} from the impulsive start u = 1 (t = " \
+             f"{(warmup + 1) * cs.dt:g}..{(warmup + args.steps) * cs.dt:g})"
+    config = {"workload": f"{cs.name}: {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]} non-uniform grid, sphere D=1, "
+                          f"Re {cs.re:g} (held out of the network's training), dt {cs.dt:g}, red-black SOR omega "
+                          f"{cs.omega:g} to FP64 residual L-inf <= {cs.eps:g}; timed window: {window}",
+              "window": window,
+              "l2": "inputs larger than L2: each step reads/writes 7 FP64 fields of 77.7 MB",
+              "parallelism": "replicas" if dist.world > 1 else "single GPU"}
 
     if args.impl == "reference":
         if dist.rank != 0:
             dist.close()
             return
-        table = sweep_table()
-        window = table[warmup:warmup + args.steps] if len(table) >= warmup + args.steps else table
-        n = sum(window) / len(window) if window else 8000.0
-        cpu = cpu_sample(pkg, cs, n, threads)
-        line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "steps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 / cpu["value"],
+        ref = reference_arm(pkg, cs, warmup, args.steps, threads, args.ref_budget)
+        n = ref["steps_timed"]
+        sample = (f"FP64 oracle (C restatement of the reference, sweep loop in its bit-identical row form, OpenMP "
+                  f"{threads} threads): {warmup} untimed warm-up steps from the impulsive start, then {n} whole "
+                  f"steps timed ({window if n == args.steps else f'steps {warmup + 1}..{warmup + n}'}), each to "
+                  f"the FP64 residual tolerance ({sum(ref['sweeps_per_step']) / max(n, 1):.0f} sweeps per step)")
+        line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": "steps/s", "n_gpus": args.gpus,
+                "steps": n, "warmup": warmup, "ms_per_step": 1e3 * ref["seconds"] / max(n, 1),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic: icosphere body, stretched grid, impulsive start",
-                "config": {"workload": f"{cs.name} {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]}, Re {cs.re:g}, "
-                                       f"dt {cs.dt:g}, RB-SOR omega {cs.omega:g} to FP64 residual <= {cs.eps:g}",
-                           "mode": "reference algorithm in FP64 on the host cores"},
-                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
-                "e2e": {"value": cpu["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "config": dict(config, mode="reference algorithm in FP64 on the host cores"),
+                "cpu_baseline": {"value": ref["value"], "unit": "steps/s", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": ref["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "reference_detail": {k: ref[k] for k in ("seconds", "seconds_per_step", "sweeps_per_step",
+                                                         "warmup_seconds", "warmup_sweeps", "setup_seconds", "fit")},
+                "drag_lift": ref["coefs"][-1] if ref["coefs"] else None}
+        if n < args.steps:
+            line["note"] = f"the timed-work budget of {args.ref_budget:g} s stopped the arm after {n} of {args.steps} steps"
         print(json.dumps(line), flush=True)
         dist.close()
         return
 
     import torch
     torch.cuda.set_device(dist.local)
+    net = load_net(pkg, args.weights, args.coarsen) if "learned" in arms else None
 
-    if args.record_sweeps:
-        s = pkg.setup_case(cs, **PLAIN)
-        counts = []
-        for q in range(args.record_sweeps):
-            st, _ = s.step(q == 0)
-            counts.append(int(st["sweeps"]))
-            print(f"step {q + 1}: {st['sweeps']} sweeps", file=sys.stderr, flush=True)
-        s.close()
-        path = pathlib.Path(args.record_out) if args.record_out else ROOT / "oracle" / f"sweeps_{cs.name}.json"
-        path.write_text(json.dumps({"workload": cs.name, "mode": "FP64, zero warm start, residual every 8 sweeps",
-                                    "omega": cs.omega, "eps": cs.eps, "sweeps": counts}, indent=1) + "\n")
-        print(json.dumps({"recorded": str(path), "sweeps": counts}), flush=True)
+    if args.developed:
+        if dist.rank == 0:
+            print(json.dumps(developed_run(pkg, cs, args.developed, warmup, args.steps, dist, net, arms)), flush=True)
+        if net is not None:
+            net.close()
+        dist.close()
         return
 
-    arms = set(args.arms.split(","))
     # Headline: FP32 sweeps in FP64 defect correction with the learned warm start (the
     # trained network in the package); without weights, the previous-correction warm start.
-    net = load_net(pkg, args.weights, args.coarsen) if "learned" in arms else None
     head_mode = dict(FAST, warm_start=pkg.WARM_LEARNED) if net is not None else FAST
     clocks = Clocks(dist.local)
-    fast = run_arm(pkg, cs, head_mode, warmup, args.steps, dist, timers=True, clocks=clocks, net=net)
-    t = dist.max(fast["seconds"])
+    head = run_arm(pkg, cs, head_mode, warmup, args.steps, dist, timers=True, clocks=clocks, net=net)
+    t = dist.max(head["seconds"])
     value = dist.world * args.steps / t
-    tm = fast["timers"]
+    tm = head["timers"]
     ncell = cs.cells
-    sweeps = sum(st["sweeps"] for st in fast["stats"])
-    t_launch32 = tm["sor32_ms"] / max(2 * tm["sweeps32"], 1) * 1e-3
-    achieved = BYTES_SOR32_LAUNCH * ncell / t_launch32 / 1e9
+    sweeps = sum(st["sweeps"] for st in head["stats"])
+    launches32 = max(tm["launches32"], 1)
+    t_launch32 = tm["sor32_ms"] * 1e-3 / launches32
+    sweeps_per_launch = tm["sweeps32"] / launches32
+    bytes_launch = BYTES_SOR32_SWEEP * ncell * sweeps_per_launch
+    achieved = bytes_launch / t_launch32 / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s (of fallback)"
     phase_total = sum(tm[f"{p}_ms"] for p in pkg.Timers.PHASES)
+
+    def summary(r, steps):
+        tt = dist.max(r["seconds"])
+        return {"value": dist.world * steps / tt, "unit": "steps/s", "ms_per_step": 1e3 * tt / steps,
+                "sweeps_per_step": sum(st["sweeps"] for st in r["stats"]) / steps,
+                "worst_final_residual": max(st["final_err"] for st in r["stats"]), "drag_lift": r["coef"]}
 
     prev_line = None
     if net is not None and "fast" in arms:
         prv = run_arm(pkg, cs, FAST, warmup, args.steps, dist, timers=True)
-        pt = dist.max(prv["seconds"])
-        psweeps = sum(st["sweeps"] for st in prv["stats"]) / args.steps
-        prev_line = {"value": dist.world * args.steps / pt, "unit": "steps/s", "ms_per_step": 1e3 * pt / args.steps,
-                     "sweeps_per_step": psweeps, "drag_lift": prv["coef"],
-                     "learned_sweeps_saved": 1.0 - (sweeps / args.steps) / psweeps}
-    plain_steps = max(1, min(args.plain_steps, args.steps))
-    if "plain" in arms:
-        plain = run_arm(pkg, cs, PLAIN, warmup, plain_steps, dist, timers=True)
-        t_plain = dist.max(plain["seconds"])
-        plain_value = dist.world * plain_steps / t_plain
-        ptm = plain["timers"]
-        plain_sweeps = [st["sweeps"] for st in plain["stats"]]
-        t_sweep64 = ptm["sor64_ms"] / max(ptm["sweeps64"], 1) * 1e-3
-    else:
-        table = sweep_table()
-        plain_value, t_sweep64 = None, None
-        plain_sweeps = table[warmup:warmup + plain_steps] or [0]
+        prev_line = summary(prv, args.steps)
+        prev_line["learned_sweeps_saved"] = 1.0 - (sweeps / args.steps) / prev_line["sweeps_per_step"]
+    plain_runs = {}
+    for name, mode in (("plain_fp64_fast", PLAIN_FAST), ("plain_fp64", PLAIN)):
+        if (name == "plain_fp64" and "plain" in arms) or (name == "plain_fp64_fast" and "plain_fast" in arms):
+            r = run_arm(pkg, cs, mode, warmup, args.steps, dist, timers=True)
+            line_p = summary(r, args.steps)
+            ptm = r["timers"]
+            t_sweep = ptm["sor64_ms"] * 1e-3 / max(ptm["sweeps64"], 1)
+            line_p["ms_per_sweep"] = 1e3 * t_sweep
+            line_p["sweep_gbs_algorithmic"] = BYTES_SOR64_SWEEP * ncell / t_sweep / 1e9
+            line_p["sweep_hbm_frac"] = line_p["sweep_gbs_algorithmic"] / hbm
+            line_p["sweep_bound"] = "FP64 ALU (GB300 FP64 ~0.5 TFMA/s measured)"
+            plain_runs[name] = (r, line_p)
+    ref_run = plain_runs.get("plain_fp64", plain_runs.get("plain_fp64_fast", (None, None)))[0]
+    plain_lines = {k: v[1] for k, v in plain_runs.items()}
+    if "plain_fp64_fast" in plain_runs and "plain_fp64" in plain_runs:
+        plain_lines["plain_fp64_fast"]["vs_plain_fp64"] = coef_errors(plain_runs["plain_fp64_fast"][0]["coefs"],
+                                                                      plain_runs["plain_fp64"][0]["coefs"])
+    plain_values = [v["value"] for v in plain_lines.values()]
 
     if "e2e" in arms:
         e2e = run_e2e(pkg, cs, head_mode, warmup, args.steps, dist, net=net)
@@ -691,56 +849,57 @@ def main():
     else:
         e2e, e2e_value = {"h2d": None, "d2h": None}, None
 
+    errs = coef_errors(head["coefs"], ref_run["coefs"]) if ref_run is not None else None
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f64",
         "data": "synthetic: icosphere body (2562 nodes, 5120 triangles), stretched grid, impulsive start u=1",
-        "config": {"workload": f"{cs.name}: {cs.shape[0]}x{cs.shape[1]}x{cs.shape[2]} non-uniform grid, sphere D=1, "
-                               f"Re {cs.re:g}, dt {cs.dt:g}, red-black SOR omega {cs.omega:g} to FP64 residual "
-                               f"L-inf <= {cs.eps:g}",
-                   "mode": (f"FP32 red-black sweeps inside FP64 defect correction, inner relaxation "
-                            f"{FAST['omega_inner']:g}, "
-                            + (f"learned warm start (BF16 U-Net on the {net.coarsen}x{net.coarsen}x{net.coarsen}"
-                               f"-coarsened domain, weights ib3d-gpu_gb300/weights/{net.weights})" if net is not None
-                               else "warm start from the previous step's correction")),
-                   "inner_sweeps": FAST["inner_sweeps"],
-                   "inner_schedule": "passes of inner_sweeps FP32 sweeps between FP64 residual checks; the last "
-                                     "pass cut to the sweeps the measured rate needs" if FAST.get("inner_schedule") == 2
-                                     else "fixed passes",
-                   "l2": "inputs larger than L2: each step reads/writes 7 FP64 fields of 77.7 MB",
-                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-        "plain_fp64": {"value": plain_value, "unit": "steps/s", "steps": plain_steps,
-                       "sweeps_per_step": sum(plain_sweeps) / len(plain_sweeps),
-                       "ms_per_sweep": t_sweep64 * 1e3 if t_sweep64 else None,
-                       "sweep_bound": "FP64 ALU (GB300 FP64 ~0.5 TFMA/s measured)"},
-        "speedup_vs_plain_fp64": value / plain_value if plain_value else None,
+        "config": dict(config, mode=(f"FP32 red-black sweeps inside FP64 defect correction, inner relaxation "
+                                     f"{FAST['omega_inner']:g}, "
+                                     + (f"learned warm start (BF16 U-Net on the {net.coarsen}x{net.coarsen}x"
+                                        f"{net.coarsen}-coarsened domain, weights ib3d-gpu_gb300/weights/"
+                                        f"{net.weights})" if net is not None
+                                        else "warm start from the previous step's correction")),
+                       inner_sweeps=FAST["inner_sweeps"],
+                       inner_schedule=("passes of inner_sweeps FP32 sweeps between FP64 residual checks; the "
+                                       "last pass cut to the sweeps the measured rate needs")
+                       if FAST.get("inner_schedule") == 2 else "fixed passes"),
+        "worst_final_residual": max(st["final_err"] for st in head["stats"]),
+        "drag_rel_vs_fp64": errs["drag_rel"] if errs else None,
+        "lift_rel_vs_fp64": errs["lift_rel"] if errs else None,
+        "fp64_reference_arm": ("plain_fp64" if "plain_fp64" in plain_runs else "plain_fp64_fast") if errs else None,
+        **plain_lines,
+        "speedup_vs_plain_fp64": value / plain_lines["plain_fp64"]["value"] if "plain_fp64" in plain_lines else None,
+        "speedup_vs_fastest_plain": value / max(plain_values) if plain_values else None,
         "fp32_previous_correction": prev_line,
         "net_ms_per_step": tm["net_ms"] / args.steps,
         "sweeps_per_step": sweeps / args.steps,
         "sweeps_per_s": tm["sweeps32"] / (tm["sor32_ms"] * 1e-3) if tm["sor32_ms"] else None,
         "cells_per_s": value * ncell,
         "phase_ms_per_step": {p: tm[f"{p}_ms"] / args.steps for p in pkg.Timers.PHASES},
-        "drag_lift": fast["coef"],
-        "roofline": {"kernel": "k_sor32p (one colour pass of the FP32 red-black sweep, colour-packed)",
-                     "bound": "hbm", "achieved": achieved,
-                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic_per_launch(cs),
-                     "traffic_cold": traffic_per_launch(cs, cold=True),
-                     "note": "the packed arrays (76 MB) stay in L2 inside the sweep loop: DRAM traffic is the "
-                             "warm-cache figure; the pass is bound by the L1 data pipe (71 % of peak while "
-                             "active), so frac is a rate of algorithmic bytes against the HBM peak",
-                     "bytes_per_launch": BYTES_SOR32_LAUNCH * ncell, "cells": ncell,
-                     "ms_per_launch": t_launch32 * 1e3,
+        "drag_lift": head["coef"],
+        "roofline": {"kernel": "k_sor32p (FP32 red-black sweep, colour-packed; one launch per colour pass)",
+                     "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": DRAM_BYTES_PER_CELL_SWEEP32 * ncell * sweeps_per_launch,
+                     "traffic_cold": DRAM_BYTES_PER_CELL_SWEEP32_COLD * ncell * sweeps_per_launch,
+                     "bytes_per_launch": bytes_launch, "bytes_per_cell_sweep": BYTES_SOR32_SWEEP,
+                     "sweeps_per_launch": sweeps_per_launch, "cells": ncell, "ms_per_launch": t_launch32 * 1e3,
+                     "us_per_sweep": 1e6 * tm["sor32_ms"] * 1e-3 / max(tm["sweeps32"], 1),
                      "share_of_step": tm["sor32_ms"] / phase_total if phase_total else None,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+                     "peak_source": peak_src},
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
         "gpu_launches": tm["launches"],
-        "clocks": fast["clocks"],
+        "clocks": head["clocks"],
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu and "cpu" in arms:
-        cpu = cpu_sample(pkg, cs, sum(plain_sweeps) / len(plain_sweeps), threads)
-        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if plain_lines:
+            n_plain = next(iter(plain_lines.values()))["sweeps_per_step"]
+            if "plain_fp64" in plain_lines:
+                n_plain = plain_lines["plain_fp64"]["sweeps_per_step"]
+            cpu = cpu_sample(pkg, cs, n_plain, threads)
+            line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     if net is not None:
         net.close()
     if dist.rank == 0:

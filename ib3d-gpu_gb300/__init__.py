@@ -29,7 +29,7 @@ HEADER = HERE.parent / "include" / "ib3d.h"
 OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_PROBE, ERR_NOCONV, ERR_NONFINITE, ERR_MEMORY, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ERR_IO = -9
 CRIT_UPDATE, CRIT_RESIDUAL = 0, 1
-PREC_FP64, PREC_FP32DC = 0, 1
+PREC_FP64, PREC_FP32DC, PREC_FP64_FAST = 0, 1, 2
 WARM_ZERO, WARM_PREV, WARM_LEARNED = 0, 1, 2
 INNER_FIXED, INNER_ADAPTIVE, INNER_TAIL = 0, 1, 2
 MESH_GMSH, MESH_GAMBIT = 0, 1
@@ -66,12 +66,12 @@ class SolveStats(C.Structure):
 
 class Timers(C.Structure):
     _fields_ = [("ms", C.c_double * 10), ("sweeps64", C.c_int64), ("sweeps32", C.c_int64), ("outer", C.c_int64),
-                ("launches", C.c_int64), ("steps", C.c_int64)]
+                ("launches", C.c_int64), ("steps", C.c_int64), ("launches32", C.c_int64)]
     PHASES = ("momentum", "bc", "forcing", "divergence", "sor64", "sor32", "residual", "correct", "stress", "net")
 
     def as_dict(self) -> dict:
         d = {f"{n}_ms": self.ms[q] for q, n in enumerate(self.PHASES)}
-        for k in ("sweeps64", "sweeps32", "outer", "launches", "steps"):
+        for k in ("sweeps64", "sweeps32", "outer", "launches", "steps", "launches32"):
             d[k] = getattr(self, k)
         return d
 

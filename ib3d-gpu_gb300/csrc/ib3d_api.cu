@@ -255,12 +255,19 @@ int alloc_fields(ib3d_ctx* c) {
 bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
-         (p->precision == 0 || p->precision == 1) && (p->warm_start >= 0 && p->warm_start <= 2) &&
+         (p->precision >= IB3D_PREC_FP64 && p->precision <= IB3D_PREC_FP64_FAST) && (p->warm_start >= 0 && p->warm_start <= 2) &&
          p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
          (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 && p->ramp_sweeps >= 0 &&
          (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&
          (p->momentum == IB3D_MOMENTUM_EULER || p->momentum == IB3D_MOMENTUM_AB2);
+}
+
+// The sweep loop of the context's precision mode.
+int run_sor(ib3d_ctx* c, ib3d_solve_stats* st) {
+  if (c->prm.precision == IB3D_PREC_FP32DC) return run_sor_fp32dc(c, st);
+  if (c->prm.precision == IB3D_PREC_FP64_FAST) return run_sor_fp64_fast(c, st);
+  return run_sor_fp64(c, st);
 }
 
 int fail(ib3d_ctx* c, int code, const char* msg) {
@@ -495,7 +502,8 @@ void ib3d_destroy(ib3d_ctx* c) {
   void* ptrs[] = {c->d_tables, c->d_tables32, c->d_fast, c->d_axp, c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p, c->pc, c->b, c->bdt,
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
-                  c->hist[0], c->hist[1], c->r_hist, c->d_norm, c->d_norm_part, c->resi[0], c->resi[1], c->resi[2]};
+                  c->hist[0], c->hist[1], c->r_hist, c->d_norm, c->d_norm_part, c->resi[0], c->resi[1], c->resi[2],
+                  c->wdiag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -702,7 +710,7 @@ int ib3d_timers_enable(ib3d_ctx* c, int on) {
   timer_fold(c);
   if (on) {
     for (double& x : c->tms) x = 0.0;
-    c->t_sweeps64 = c->t_sweeps32 = c->t_outer = c->t_steps = 0;
+    c->t_sweeps64 = c->t_sweeps32 = c->t_outer = c->t_steps = c->t_launches32 = 0;
     c->launches = 0;
   }
   c->timing = on != 0;
@@ -718,6 +726,7 @@ int ib3d_timers_read(ib3d_ctx* c, ib3d_timers* out) {
   out->sweeps32 = c->t_sweeps32;
   out->outer = c->t_outer;
   out->launches = c->launches;
+  out->launches32 = c->t_launches32;
   out->steps = c->t_steps;
   return IB3D_OK;
 }
@@ -730,7 +739,7 @@ int ib3d_synchronize(ib3d_ctx* c) {
 
 int ib3d_ns_momentum(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
-  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c, false);
+  if (c->prm.precision != IB3D_PREC_FP64) launch_momentum_fast(c, false);
   else launch_momentum(c, false);
   IB3D_CUDA(c, cudaGetLastError());
   return IB3D_OK;
@@ -739,7 +748,7 @@ int ib3d_ns_momentum(ib3d_ctx* c) {
 int ib3d_ns_momentum_ab(ib3d_ctx* c) {
   if (!c) return IB3D_ERR_ARG;
   if (int rc = ensure_resi(c, true)) return rc;
-  if (c->prm.precision == IB3D_PREC_FP32DC) launch_momentum_fast(c, true);
+  if (c->prm.precision != IB3D_PREC_FP64) launch_momentum_fast(c, true);
   else launch_momentum(c, true);
   IB3D_CUDA(c, cudaGetLastError());
   return IB3D_OK;
@@ -816,7 +825,7 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
   IB3D_CUDA(c, cudaMemsetAsync(red, 0, 2 * sizeof(unsigned long long), c->st));
   // divergence writes its max into ctl->aux; copy it aside before the SOR resets ctl
   IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
-  if (c->prm.precision == IB3D_PREC_FP32DC) launch_divergence_fast(c, c->prm.warm_start == IB3D_WARM_ZERO);
+  if (c->prm.precision != IB3D_PREC_FP64) launch_divergence_fast(c, c->prm.warm_start == IB3D_WARM_ZERO);
   else launch_divergence(c, c->prm.warm_start == IB3D_WARM_ZERO);
   if (c->r_hist) {
     PhaseScope ps(c, PH_NET);
@@ -831,7 +840,7 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->st);
-  int rc = c->prm.precision == IB3D_PREC_FP32DC ? run_sor_fp32dc(c, &st) : run_sor_fp64(c, &st);
+  int rc = run_sor(c, &st);
   cudaEventRecord(e1, c->st);
   if (rc == IB3D_OK || rc == IB3D_ERR_NOCONV) {
     launch_correct(c);
@@ -870,7 +879,7 @@ int ib3d_redblack_sor(ib3d_ctx* c, ib3d_solve_stats* stats) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->st);
-  const int rc = c->prm.precision == IB3D_PREC_FP32DC ? run_sor_fp32dc(c, &st) : run_sor_fp64(c, &st);
+  const int rc = run_sor(c, &st);
   cudaEventRecord(e1, c->st);
   const cudaError_t ce = cudaStreamSynchronize(c->st);
   float ms = 0.f;

@@ -131,6 +131,9 @@ struct ib3d_ctx {
   // only when ib3d_params.momentum is IB3D_MOMENTUM_AB2
   double* resi[3] = {nullptr, nullptr, nullptr};
   float *e32 = nullptr, *r32 = nullptr;
+  // omega/diag(A) per fluid cell (0 elsewhere) for the fast plain FP64 sweep
+  // (IB3D_PREC_FP64_FAST); allocated on its first solve, refilled at every solve
+  double* wdiag = nullptr;
   // colour-packed FP32 arrays of the inner solve ([0] red, [1] black); see k_sor32.cu
   float* ep[2] = {nullptr, nullptr};
   float* rp[2] = {nullptr, nullptr};
@@ -194,7 +197,7 @@ struct ib3d_ctx {
   std::vector<EvPair> pending;
   std::vector<cudaEvent_t> pool;
   double tms[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  long long t_sweeps64 = 0, t_sweeps32 = 0, t_outer = 0, t_steps = 0;
+  long long t_sweeps64 = 0, t_sweeps32 = 0, t_outer = 0, t_steps = 0, t_launches32 = 0;
   long long launches = 0;
 };
 
@@ -207,6 +210,7 @@ void launch_divergence_fast(ib3d_ctx* c, bool zero_pc);
 void launch_residual_fast(ib3d_ctx* c, long long sweep);
 void launch_bdt(ib3d_ctx* c, bool zero_pc);
 int run_sor_fp64(ib3d_ctx* c, ib3d_solve_stats* st);
+int run_sor_fp64_fast(ib3d_ctx* c, ib3d_solve_stats* st);
 int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st);
 void launch_correct(ib3d_ctx* c);
 void launch_velocity_bc(ib3d_ctx* c);

@@ -85,12 +85,72 @@ __global__ void __launch_bounds__(kBlock) k_residual_fast(Dims d, Grid1D g, cons
     if (rp_red) {
       const long long sp = ((long long)(k - 1) * d.NY2 + (j - 1)) * Lp + ((i - 2) >> 1) + 4;
       (((i + j + k) & 1) ? rp_red : rp_black)[sp] = rr;
-    } else {
+    } else if (r32) {   // neither: a convergence check of the fast plain FP64 path
       r32[idx] = rr;
     }
   }
   block_max_atomic(m, &ctl->res);
   finish_block(ctl, &ctl->res, 0, sweep, eps, max_sweeps);
+}
+
+// omega/diag(A) at the fluid cells, 0 elsewhere: the factor of the fast plain FP64
+// sweep, one IEEE division per cell per solve instead of one per cell per sweep.
+__global__ void __launch_bounds__(kBlock) k_wdiag(Dims d, Grid1D g, const unsigned char* __restrict__ cell,
+                                                  double omega, double* __restrict__ wd) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)d.n3) return;
+  const int i = (int)(tid % (unsigned)d.NX2) + 1;
+  const unsigned t = tid / (unsigned)d.NX2;
+  const int j = (int)(t % (unsigned)d.NY2) + 1, k = (int)(t / (unsigned)d.NY2) + 1;
+  double w = 0.0;
+  if (i >= 2 && i <= d.nx + 1 && j >= 2 && j <= d.ny + 1 && k >= 2 && k <= d.nz + 1 && cell[tid] == 0)
+    w = omega / (g.acx[1][i - 1] + g.acy[1][j - 1] + g.acz[1][k - 1]);
+  wd[tid] = w;
+}
+
+// One colour of the fast plain FP64 sweep (IB3D_PREC_FP64_FAST): REDBLACKSOR's
+// update (subPcorVcor.f90:164-191), pc <- (1-omega) pc + omega (b/dt - sum A_nb
+// pc_nb) / diag, as six contracted multiply-adds, one product and one multiply-add
+// with wd = omega/diag (8 FP64 operations a cell against the reference
+// arithmetic's ~18 and a division). Red cells are (i+j+k) odd (subSearch.f90:562);
+// each thread owns one (i, i+1) pair of a row. DELTA: the update norm max |pc_new -
+// pc_old| (IB3D_CRIT_UPDATE) is reduced on chip and decided after the black pass;
+// the residual test needs no update norm, so that form skips it.
+template <int COLOR, bool DELTA>
+__global__ void __launch_bounds__(kBlock) k_sor64_fast(Dims d, Grid1D g, const double* __restrict__ bdt,
+                                                       const double* __restrict__ wd, double* __restrict__ pc,
+                                                       double om1, SolveCtl* ctl, long long sweep,
+                                                       int decide_mode, double eps, long long max_sweeps) {
+  if (ctl->done) return;
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned npairs = (unsigned)(d.nx + 1) >> 1;
+  double delta = 0.0;
+  if (tid < npairs * (unsigned)d.ny * (unsigned)d.nz) {
+    const int ip = (int)(tid % npairs);
+    const unsigned t = tid / npairs;
+    const int j = (int)(t % (unsigned)d.ny) + 2, k = (int)(t / (unsigned)d.ny) + 2;
+    const int i0 = 2 + 2 * ip;
+    const int i = i0 + ((i0 + j + k + 1 + COLOR) & 1);
+    if (i <= d.nx + 1) {
+      const long long idx = d.at(i, j, k);
+      const double w = wd[idx];
+      if (w != 0.0) {
+        const long long sy = d.NX2, sz = (long long)d.NX2 * d.NY2;
+        double num = fma(-g.acx[0][i - 1], pc[idx - 1], bdt[idx]);
+        num = fma(-g.acx[2][i - 1], pc[idx + 1], num);
+        num = fma(-g.acy[0][j - 1], pc[idx - sy], num);
+        num = fma(-g.acy[2][j - 1], pc[idx + sy], num);
+        num = fma(-g.acz[0][k - 1], pc[idx - sz], num);
+        num = fma(-g.acz[2][k - 1], pc[idx + sz], num);
+        const double old = pc[idx];
+        const double nw = fma(w, num, om1 * old);
+        pc[idx] = nw;
+        if (DELTA) delta = fabs(nw - old);
+      }
+    }
+  }
+  if (DELTA) block_max_atomic(delta, &ctl->upd);
+  if (COLOR == 1) finish_block(ctl, &ctl->upd, decide_mode, sweep, eps, max_sweeps);
 }
 
 // r = ((b/dt) - A pc) / diag(A) at the fluid cells (the FP64 residual of the defect
@@ -251,6 +311,59 @@ void launch_divergence_fast(ib3d_ctx* c, bool zero_pc) {
   k_divergence_fast<<<nblk(c->d.n3), kBlock, 0, c->st>>>(c->d, c->d_fast, c->fast_stride, c->ut, c->vt, c->wt,
                                                          c->cell, c->b, c->bdt, c->pc, 1.0 / c->prm.deltat,
                                                          zero_pc ? 1 : 0, &c->ctl->aux);
+}
+
+// REDBLACKSOR in the fast plain FP64 form: the loop of run_sor_fp64 (batches of
+// sweeps between host reads of the device-side decision; the residual test every
+// check_every sweeps, or the update norm every sweep) around k_sor64_fast.
+int run_sor_fp64_fast(ib3d_ctx* c, ib3d_solve_stats* st) {
+  const Dims& d = c->d;
+  const ib3d_params& P = c->prm;
+  const unsigned gcol = nblk((((long long)d.nx + 1) / 2) * d.ny * d.nz);
+  const long long ncell = (long long)d.nx * d.ny * d.nz;
+  const bool resid = P.criterion == IB3D_CRIT_RESIDUAL;
+  const int every = P.check_every < 1 ? 1 : P.check_every;
+  if (!c->wdiag) IB3D_CUDA(c, cudaMalloc(&c->wdiag, (size_t)d.n3 * sizeof(double)));
+  c->launches += 1;
+  k_wdiag<<<nblk(d.n3), kBlock, 0, c->st>>>(d, c->g, c->cell, P.omega, c->wdiag);
+  IB3D_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(SolveCtl), c->st));
+  const double om1 = 1.0 - P.omega;
+  long long sweep = 0, batch = 4;
+  for (;;) {
+    {
+      PhaseScope ps(c, PH_SOR64);
+      for (long long q = 0; q < batch; ++q) {
+        ++sweep;
+        const bool check = resid && (sweep % every) == 0;
+        c->launches += check ? 3 : 2;
+        if (resid) {
+          k_sor64_fast<0, false><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->wdiag, c->pc, om1, c->ctl, sweep, 2,
+                                                             P.eps, P.max_sweeps);
+          k_sor64_fast<1, false><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->wdiag, c->pc, om1, c->ctl, sweep,
+                                                             check ? 2 : 1, P.eps, P.max_sweeps);
+          if (check)
+            k_residual_fast<<<nblk(ncell), kBlock, 0, c->st>>>(d, c->g, c->bdt, c->pc, c->cell, nullptr, nullptr,
+                                                               nullptr, 0, c->ctl, sweep, P.eps, P.max_sweeps);
+        } else {
+          k_sor64_fast<0, true><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->wdiag, c->pc, om1, c->ctl, sweep, 2,
+                                                            P.eps, P.max_sweeps);
+          k_sor64_fast<1, true><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->bdt, c->wdiag, c->pc, om1, c->ctl, sweep, 0,
+                                                            P.eps, P.max_sweeps);
+        }
+      }
+    }
+    IB3D_CUDA(c, cudaGetLastError());
+    IB3D_CUDA(c, cudaMemcpyAsync(c->h_ctl, c->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, c->st));
+    IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+    if (c->h_ctl->done) break;
+    if (batch < 256) batch *= 2;
+  }
+  st->sweeps = c->h_ctl->nsweeps;
+  st->outer = 0;
+  c->t_sweeps64 += st->sweeps;
+  st->final_err = c->h_ctl->final_err;
+  if (c->h_ctl->final_err != c->h_ctl->final_err) return IB3D_ERR_NONFINITE;
+  return c->h_ctl->done == 2 ? IB3D_ERR_NOCONV : IB3D_OK;
 }
 
 void launch_residual_fast(ib3d_ctx* c, long long sweep) {

@@ -515,6 +515,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     {
       PhaseScope ps(c, PH_SOR32);
       c->launches += 2 * batch;
+      c->t_launches32 += 2 * batch;
       for (int q = 0; q < batch; ++q) {
         // the solve's first sweeps run at relaxation 1 (smooth_sweeps: Gauss-Seidel damps the
         // high-frequency error that the over-relaxed sweeps barely touch), the next

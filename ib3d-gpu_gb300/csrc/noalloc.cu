@@ -40,7 +40,8 @@ constexpr int kMaxDevices = 64;
 unsigned char* g_addr[kMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up on the first
-// call made on that device and cached.
+// call made on that device and cached. A call that meets any CUDA error drops the
+// cached address (forget_scratch_address), so the next call looks it up again.
 cudaError_t scratch_on_current_device(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -55,6 +56,13 @@ cudaError_t scratch_on_current_device(unsigned char** out) {
   }
   *out = g_addr[dev];
   return cudaSuccess;
+}
+
+void forget_scratch_address() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_mu);
+  g_addr[dev] = nullptr;
 }
 
 struct Coefs {  // the caller's (n,3) column-major Acx/Acy/Acz (device)
@@ -149,27 +157,15 @@ __global__ void k_na_accumulate(long long n3, double* __restrict__ pc, float* __
   }
 }
 
-}  // namespace
-}  // namespace ib3d
 
-using namespace ib3d;
-
-extern "C" int ib3d_pressure_solve_noalloc(int64_t nx, int64_t ny, int64_t nz, const double* acx, const double* acy,
-                                           const double* acz, const unsigned char* cell, const double* b,
-                                           double deltat, double* pc, double omega, double eps,
-                                           int64_t max_sweeps, int32_t inner_sweeps, void* stream,
-                                           int64_t* sweeps_out, double* residual_out) {
-  if (nx < 4 || ny < 4 || nz < 4 || !acx || !acy || !acz || !cell || !b || !pc || !(deltat > 0) ||
-      !(omega > 0 && omega < 2) || !(eps > 0) || max_sweeps < 1 || inner_sweeps < 1)
-    return IB3D_ERR_ARG;
+int run_noalloc(int64_t nx, int64_t ny, int64_t nz, const double* acx, const double* acy, const double* acz,
+                const unsigned char* cell, const double* b, double deltat, double* pc, double omega, double eps,
+                int64_t max_sweeps, int32_t inner_sweeps, cudaStream_t st, unsigned char* base,
+                int64_t* sweeps_out, double* residual_out) {
   const long long n3 = (nx + 2) * (ny + 2) * (nz + 2);
-  if (n3 > kMaxCells) return IB3D_ERR_TOO_LARGE;
-  unsigned char* base = nullptr;
-  if (scratch_on_current_device(&base) != cudaSuccess) return IB3D_ERR_CUDA;
   float* r32 = reinterpret_cast<float*>(base);
   float* e32 = reinterpret_cast<float*>(base + kArrayBytes);
   SolveCtl* ctl = reinterpret_cast<SolveCtl*>(base + kCtlOffset);
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   Dims d;
   d.nx = (int)nx; d.ny = (int)ny; d.nz = (int)nz;
   d.NX2 = d.nx + 2; d.NY2 = d.ny + 2; d.NZ2 = d.nz + 2;
@@ -203,4 +199,32 @@ extern "C" int ib3d_pressure_solve_noalloc(int64_t nx, int64_t ny, int64_t nz, c
   if (residual_out) *residual_out = h.final_err;
   if (h.final_err != h.final_err) return IB3D_ERR_NONFINITE;
   return h.done == 2 ? IB3D_ERR_NOCONV : IB3D_OK;
+}
+}  // namespace
+}  // namespace ib3d
+
+using namespace ib3d;
+
+extern "C" int ib3d_pressure_solve_noalloc(int64_t nx, int64_t ny, int64_t nz, const double* acx, const double* acy,
+                                           const double* acz, const unsigned char* cell, const double* b,
+                                           double deltat, double* pc, double omega, double eps,
+                                           int64_t max_sweeps, int32_t inner_sweeps, void* stream,
+                                           int64_t* sweeps_out, double* residual_out) {
+  if (nx < 4 || ny < 4 || nz < 4 || !acx || !acy || !acz || !cell || !b || !pc || !(deltat > 0) ||
+      !(omega > 0 && omega < 2) || !(eps > 0) || max_sweeps < 1 || inner_sweeps < 1)
+    return IB3D_ERR_ARG;
+  // each extent is bounded before the product is formed, so the product cannot overflow
+  if (nx > kMaxCells || ny > kMaxCells || nz > kMaxCells) return IB3D_ERR_TOO_LARGE;
+  if ((nx + 2) * (ny + 2) > kMaxCells) return IB3D_ERR_TOO_LARGE;
+  const long long n3 = (nx + 2) * (ny + 2) * (nz + 2);
+  if (n3 > kMaxCells) return IB3D_ERR_TOO_LARGE;
+  unsigned char* base = nullptr;
+  if (scratch_on_current_device(&base) != cudaSuccess) {
+    forget_scratch_address();
+    return IB3D_ERR_CUDA;
+  }
+  const int rc = run_noalloc(nx, ny, nz, acx, acy, acz, cell, b, deltat, pc, omega, eps, max_sweeps, inner_sweeps,
+                             static_cast<cudaStream_t>(stream), base, sweeps_out, residual_out);
+  if (rc == IB3D_ERR_CUDA) forget_scratch_address();
+  return rc;
 }

@@ -117,6 +117,38 @@ int ib3d_write_result_text(ib3d_ctx* c, const char* path, double totime, int64_t
   return ok ? IB3D_OK : fail(c, IB3D_ERR_IO, "ib3d_write_result_text: write failed");
 }
 
+}  // extern "C"
+
+namespace {
+// One value of a list-directed record: blanks, tabs and line ends before it, and at
+// most one comma among them, separate it from the previous value.
+bool read_list_value(FILE* fp, double* out) {
+  int ch;
+  bool comma = false;
+  while ((ch = std::fgetc(fp)) != EOF) {
+    if (ch == ' ' || ch == '\t' || ch == '\n' || ch == '\r') continue;
+    if (ch == ',' && !comma) {
+      comma = true;
+      continue;
+    }
+    break;
+  }
+  if (ch == EOF) return false;
+  std::ungetc(ch, fp);
+  return std::fscanf(fp, "%lf", out) == 1;
+}
+
+// The rest of the current line: a list-directed READ that has its values skips what
+// is left of the record it stopped in.
+void skip_rest_of_record(FILE* fp) {
+  int ch;
+  while ((ch = std::fgetc(fp)) != EOF && ch != '\n') {
+  }
+}
+}  // namespace
+
+extern "C" {
+
 int ib3d_read_result_text(ib3d_ctx* c, const char* path, double* totime, int64_t* ita, int64_t* ita1) {
   if (!c || !path) return IB3D_ERR_ARG;
   FILE* fp = std::fopen(path, "r");
@@ -126,11 +158,15 @@ int ib3d_read_result_text(ib3d_ctx* c, const char* path, double* totime, int64_t
   for (auto& v : f) v.resize(n3);
   double t = 0.0, it = 0.0, it1 = 0.0;
   bool ok = true;
-  // list-directed records: separators are blanks or commas; ita, ita1 may be
-  // written as integers or reals
-  for (size_t q = 0; q < n3 && ok; ++q)
-    ok = std::fscanf(fp, " %lf%*[ ,\t] %lf%*[ ,\t] %lf%*[ ,\t] %lf%*[ ,\t] %lf%*[ ,\t] %lf%*[ ,\t] %lf", &f[0][q],
-                     &f[1][q], &f[2][q], &f[3][q], &t, &it, &it1) == 7;
+  // list-directed records (READ(1,*) u, v, w, p, totime, ita, ita1 per cell,
+  // subLastConditions.f90:24-29): values separated by blanks, a comma or line ends, so
+  // a record may continue on the next line; ita, ita1 may be written as integers or
+  // reals
+  for (size_t q = 0; q < n3 && ok; ++q) {
+    double* dst[7] = {&f[0][q], &f[1][q], &f[2][q], &f[3][q], &t, &it, &it1};
+    for (int m = 0; m < 7 && ok; ++m) ok = read_list_value(fp, dst[m]);
+    if (ok) skip_rest_of_record(fp);
+  }
   std::fclose(fp);
   if (!ok) return fail(c, IB3D_ERR_IO, "ib3d_read_result_text: fewer than (nx+2)(ny+2)(nz+2) records of 7 values");
   const int rc = ib3d_upload_fields(c, f[0].data(), f[1].data(), f[2].data(), f[3].data());

@@ -7,7 +7,7 @@
  * called from PROGRAM main (main.f90:5-67). Each entry point below replaces one
  * of those calls; the comment beside it names the reference interface
  * (file:line) it stands in for. A Fortran driver binds them with ISO_C_BINDING
- * (`bind(C)` interfaces; see INTEGRATION.md) and replaces `CALL nsMomentum` by
+ * (`bind(C)` interfaces) and replaces `CALL nsMomentum` by
  * `ierr = ib3d_ns_momentum(ctx)`, and so on.
  *
  * Types: int64_t is Fortran INTEGER(KIND=8), double is REAL(KIND=8).
@@ -49,6 +49,10 @@ extern "C" {
 /* Pressure-solve arithmetic. */
 #define IB3D_PREC_FP64 0     /* reference arithmetic, bit-identical to the FP64 oracle */
 #define IB3D_PREC_FP32DC 1   /* FP32 red-black sweeps inside an FP64 defect-correction loop */
+#define IB3D_PREC_FP64_FAST 2 /* plain FP64 method (FP64 sweeps, the reference's iteration) with
+                                 contracted multiply-adds, a precomputed omega/diag per cell instead
+                                 of the division, and reciprocal spacings in the divergence and the
+                                 predictor: differs from IB3D_PREC_FP64 by rounding only */
 
 /* Initial guess of the pressure correction pc at each step. */
 #define IB3D_WARM_ZERO 0     /* pc = 0, as subPcorVcor.f90:19-28 */
@@ -252,6 +256,8 @@ typedef struct ib3d_timers {
   int64_t outer;      /* defect-correction passes */
   int64_t launches;   /* kernels launched by the library */
   int64_t steps;      /* ib3d_step calls */
+  int64_t launches32; /* launches of the FP32 sweep kernel (one per colour pass, or one per
+                         group of fused sweeps) */
 } ib3d_timers;
 /* on != 0 clears and starts the timers; on == 0 stops them (counts are kept). */
 int ib3d_timers_enable(ib3d_ctx* ctx, int on);
@@ -344,11 +350,14 @@ int ib3d_attach_net(ib3d_ctx* ctx, ib3d_net* net);
  * reference's layout (cell as uint8). stream is a cudaStream_t or NULL.
  *
  * Limit: (nx+2)*(ny+2)*(nz+2) <= 2^21 cells (two 8 MiB FP32 arrays); larger grids
- * return IB3D_ERR_TOO_LARGE. The first call on a device looks up the scratch's device
- * address (cudaGetSymbolAddress) and caches it; make that first call before any
- * stream capture. Every call uses the same scratch and clears what must start at
- * zero, so calls that overlap on the GPU (other streams, other host threads) race:
- * serialise them. */
+ * (and any extent above 2^21) return IB3D_ERR_TOO_LARGE before any CUDA call. The
+ * first call on a device looks up the scratch's device address (cudaGetSymbolAddress)
+ * and caches it; make that first call before any stream capture. A call that meets a
+ * CUDA error drops the cached address, so the next call looks it up again. The call
+ * waits on the stream once per defect-correction pass to read the convergence
+ * decision. Every call uses the same scratch and clears what must start at zero, so
+ * calls that overlap on the GPU (other streams, other host threads) race: serialise
+ * them. */
 int ib3d_pressure_solve_noalloc(int64_t nx, int64_t ny, int64_t nz, const double* acx, const double* acy,
                                 const double* acz, const unsigned char* cell, const double* b, double deltat,
                                 double* pc, double omega, double eps, int64_t max_sweeps, int32_t inner_sweeps,

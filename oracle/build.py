@@ -23,7 +23,7 @@ def build(verbose: bool = False) -> pathlib.Path:
     if not cc:
         raise RuntimeError("no C compiler found for the oracle")
     tmp = HERE / "liboracle.so.tmp"
-    cmd = [cc, "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+    cmd = [cc, "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
            "-o", str(tmp), str(HERE / "ib3d_oracle.c"), "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

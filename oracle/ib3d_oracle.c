@@ -9,6 +9,7 @@
 #include "ib3d_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -56,6 +57,11 @@ struct OrState {
   /* stress probe caches: Elemcell, ucell, vcell, wcell, pcell (ibElems,3) */
   int64_t *scache[5];
   int have_scache;
+  /* throughput form of the sweep loop (or_set_sweep_rows): fluid mask in the field
+   * layout (1 = fluid, from cellCount) and b/deltat of the running solve */
+  int sweep_rows;
+  unsigned char* fmask;
+  double* bdt;
 };
 
 /* Fortran-style accessors. */
@@ -164,6 +170,7 @@ void or_destroy(OrState* s) {
   free(s->cell); free(s->minElemcell); free(s->e1); free(s->e2); free(s->e3);
   free(s->fluid); free(s->solid); free(s->ib); free(s->red); free(s->black); free(s->nelp);
   free(s->resi_u); free(s->resi_v); free(s->resi_w);
+  free(s->fmask); free(s->bdt);
   free(s);
 }
 
@@ -312,6 +319,12 @@ static void cell_count(OrState* s) {
     if ((i + j + k) % 2 == 1) { ++ir; L(s->red, nr, ir, 1) = i; L(s->red, nr, ir, 2) = j; L(s->red, nr, ir, 3) = k; }
     else { ++ik; L(s->black, nk, ik, 1) = i; L(s->black, nk, ik, 2) = j; L(s->black, nk, ik, 3) = k; }
   }
+  /* the same fluid set as a mask in the field layout, for the row form of the sweeps */
+  const int64_t n3 = NX2 * NY2 * (nz + 2);
+  if (!s->fmask) s->fmask = (unsigned char*)malloc((size_t)n3);
+  memset(s->fmask, 0, (size_t)n3);
+  for (int64_t n = 1; n <= nf; ++n)
+    F3(s->fmask, L(s->fluid, nf, n, 1), L(s->fluid, nf, n, 2), L(s->fluid, nf, n, 3)) = 1;
 }
 
 /* No body: every interior cell fluid (the flags tagging leaves outside its box). */
@@ -902,9 +915,12 @@ static inline double cell_residual(const OrState* s, int64_t i, int64_t j, int64
   return num - diag * F3(pc, i, j, k);
 }
 
+static int red_black_sor_rows(OrState* s, int64_t* isum_out, double* err_out);
+
 /* REDBLACKSOR (subPcorVcor.f90:148-212). Returns 0 on convergence, 1 when
  * max_sweeps ran out (the reference loops forever instead). */
 static int red_black_sor(OrState* s, int64_t* isum_out, double* err_out) {
+  if (s->sweep_rows) return red_black_sor_rows(s, isum_out, err_out);
   const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
   const double omega = s->omega, deltat = s->deltat;
   double* pc = s->pc;
@@ -961,6 +977,159 @@ static int red_black_sor(OrState* s, int64_t* isum_out, double* err_out) {
   }
   *isum_out = isum;
   *err_out = err;
+  return 0;
+}
+
+/* The same sweep loop as red_black_sor, for the timed CPU baseline: each colour pass
+ * walks the rows (j,k) of the field and updates that colour's fluid cells (the mask
+ * cellCount built) instead of gathering through the int64 red/black lists, so the
+ * OpenMP threads stream contiguous memory. Every cell's arithmetic is the list form's,
+ * expression for expression, and the values it reads are the same: a red cell's
+ * neighbours are black or non-fluid, so pco there equals pc; a cell's own pco equals
+ * its pc until its colour pass writes it, so the update-norm max |pc - pco| is taken
+ * as each cell is written, and the pco copy pass drops out. b/deltat is divided once
+ * per solve (the same quotient the list form rounds in every sweep). Results, sweep
+ * counts included, are bit-identical to red_black_sor's (tests/test_oracle.py). */
+static int red_black_sor_rows(OrState* s, int64_t* isum_out, double* err_out) {
+  const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
+  const int64_t sy = NX2, sz = NX2 * NY2, n3 = sz * (nz + 2);
+  const double omega = s->omega, deltat = s->deltat;
+  double* pc = s->pc;
+  const unsigned char* fm = s->fmask;
+  if (!s->bdt) s->bdt = (double*)malloc((size_t)n3 * sizeof(double));
+  double* bdt = s->bdt;
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < n3; ++q) bdt[q] = s->b[q] / deltat;
+  const double *ax1 = s->Acx, *ax2 = s->Acx + nx, *ax3 = s->Acx + 2 * nx;
+  const double *ay1 = s->Acy, *ay2 = s->Acy + ny, *ay3 = s->Acy + 2 * ny;
+  const double *az1 = s->Acz, *az2 = s->Acz + nz, *az3 = s->Acz + 2 * nz;
+  int64_t isum = 0;
+  double err = 0.0;
+  for (;;) {
+    ++isum;
+    double derr2 = 0.0;
+    for (int colour = 1; colour >= 0; --colour) {   /* red ((i+j+k) odd) first, then black */
+#pragma omp parallel for collapse(2) schedule(static) reduction(max : derr2)
+      for (int64_t k = 2; k <= nz + 1; ++k)
+        for (int64_t j = 2; j <= ny + 1; ++j) {
+          const int64_t i0 = ((2 + j + k) % 2 == colour) ? 2 : 3;
+          const int64_t row = (j - 1) * sy + (k - 1) * sz;
+          const double ya = ay1[j - 2], yc = ay3[j - 2], za = az1[k - 2], zc = az3[k - 2];
+          const double dyz2 = ay2[j - 2], dz2 = az2[k - 2];
+          double dmax = derr2;
+          for (int64_t i = i0; i <= nx + 1; i += 2) {
+            const int64_t o = row + (i - 1);
+            if (!fm[o]) continue;
+            const double g = (bdt[o] - ax1[i - 2] * pc[o - 1] - ax3[i - 2] * pc[o + 1] - ya * pc[o - sy] -
+                              yc * pc[o + sy] - za * pc[o - sz] - zc * pc[o + sz]) /
+                             (ax2[i - 2] + dyz2 + dz2);
+            const double old = pc[o];
+            const double nv = (1.0 - omega) * old + omega * g;
+            pc[o] = nv;
+            const double d = fabs(nv - old);
+            if (d > dmax) dmax = d;
+          }
+          derr2 = dmax;
+        }
+    }
+    if (s->criterion == 0) {
+      err = derr2;
+      if (!(derr2 >= s->eps)) break;                            /* :210 */
+    } else if (isum % s->check_every == 0) {
+      double rmax = 0.0;
+#pragma omp parallel for collapse(2) schedule(static) reduction(max : rmax)
+      for (int64_t k = 2; k <= nz + 1; ++k)
+        for (int64_t j = 2; j <= ny + 1; ++j) {
+          double m = rmax;
+          for (int64_t i = 2; i <= nx + 1; ++i) {
+            if (!F3(fm, i, j, k)) continue;
+            const double r = fabs(cell_residual(s, i, j, k, F3(bdt, i, j, k)));
+            if (r > m) m = r;
+          }
+          rmax = m;
+        }
+      err = rmax;
+      if (!(rmax >= s->eps)) break;
+    }
+    if (isum >= s->max_sweeps) { *isum_out = isum; *err_out = err; return 1; }
+  }
+  *isum_out = isum;
+  *err_out = err;
+  return 0;
+}
+
+void or_set_sweep_rows(OrState* s, int on) { s->sweep_rows = on ? 1 : 0; }
+
+/* writeResult (subWriteOutput.f90:62-72): one list-directed record
+ * "u v w p totime ita ita1" per cell, k outer, j, i inner. Values are written with
+ * 17 significant digits, so every double reads back exactly. */
+int or_write_result_text(OrState* s, const char* path, double totime, int64_t ita, int64_t ita1) {
+  FILE* fp = fopen(path, "w");
+  if (!fp) return 1;
+  int ok = 1;
+  for (int64_t k = 1; k <= s->nz + 2 && ok; ++k)
+    for (int64_t j = 1; j <= s->ny + 2 && ok; ++j)
+      for (int64_t i = 1; i <= s->nx + 2 && ok; ++i)
+        ok = fprintf(fp, " %.17g %.17g %.17g %.17g %.17g %lld %lld\n", F3(s->u, i, j, k), F3(s->v, i, j, k),
+                     F3(s->w, i, j, k), F3(s->p, i, j, k), totime, (long long)ita, (long long)ita1) > 0;
+  if (fclose(fp) != 0) ok = 0;
+  return ok ? 0 : 1;
+}
+
+/* Next value of a list-directed record: blanks, tabs, line ends and at most one
+ * comma separate values, so a record may continue on the following lines. */
+static int list_value(FILE* fp, double* out) {
+  int ch, comma = 0;
+  while ((ch = fgetc(fp)) != EOF) {
+    if (ch == ' ' || ch == '\t' || ch == '\n' || ch == '\r') continue;
+    if (ch == ',' && !comma) { comma = 1; continue; }
+    break;
+  }
+  if (ch == EOF) return 0;
+  char buf[64];
+  int n = 0;
+  while (ch != EOF && ch != ' ' && ch != '\t' && ch != '\n' && ch != '\r' && ch != ',' && n < 63) {
+    buf[n++] = (char)ch;
+    ch = fgetc(fp);
+  }
+  if (ch != EOF) ungetc(ch, fp);
+  buf[n] = 0;
+  char* end = NULL;
+  *out = strtod(buf, &end);
+  return n > 0 && end == buf + n;
+}
+
+/* lastConditions (subLastConditions.f90:2-42): resi_u/v/w = 0 (:15-17), then
+ * READ(1,*) u, v, w, p, totime, ita, ita1 for every cell in the order writeResult
+ * wrote them (:23-29; each READ starts a new record and drops what is left of the
+ * line), then ut = u, vt = v, wt = w (:32-38). Returns 1 on a short or malformed file. */
+int or_read_result_text(OrState* s, const char* path, double* totime, int64_t* ita, int64_t* ita1) {
+  FILE* fp = fopen(path, "r");
+  if (!fp) return 1;
+  const int64_t n3 = NX2 * NY2 * (s->nz + 2);
+  memset(s->resi_u, 0, (size_t)n3 * sizeof(double));
+  memset(s->resi_v, 0, (size_t)n3 * sizeof(double));
+  memset(s->resi_w, 0, (size_t)n3 * sizeof(double));
+  double t = 0.0, it = 0.0, it1 = 0.0;
+  int ok = 1;
+  for (int64_t k = 1; k <= s->nz + 2 && ok; ++k)
+    for (int64_t j = 1; j <= s->ny + 2 && ok; ++j)
+      for (int64_t i = 1; i <= s->nx + 2 && ok; ++i) {
+        ok = list_value(fp, &F3(s->u, i, j, k)) && list_value(fp, &F3(s->v, i, j, k)) &&
+             list_value(fp, &F3(s->w, i, j, k)) && list_value(fp, &F3(s->p, i, j, k)) && list_value(fp, &t) &&
+             list_value(fp, &it) && list_value(fp, &it1);
+        int ch;
+        while (ok && (ch = fgetc(fp)) != EOF && ch != '\n') {
+        }
+      }
+  fclose(fp);
+  if (!ok) return 1;
+  memcpy(s->ut, s->u, (size_t)n3 * sizeof(double));
+  memcpy(s->vt, s->v, (size_t)n3 * sizeof(double));
+  memcpy(s->wt, s->w, (size_t)n3 * sizeof(double));
+  if (totime) *totime = t;
+  if (ita) *ita = (int64_t)it;
+  if (ita1) *ita1 = (int64_t)it1;
   return 0;
 }
 

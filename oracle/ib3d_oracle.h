@@ -110,6 +110,15 @@ double* or_acoef(OrState* s, int axis);     /* (n,3) col-major Acx/Acy/Acz */
 double* or_conv_coef(OrState* s, int fam, int m);
 double* or_grid1d(OrState* s, int which);   /* 0 x1,1 y1,2 z1,3 dx,4 dy,5 dz, 6.. xu yu zu xv yv zv xw yw zw xp yp zp */
 void or_set_threads(int n);
+/* Row form of the sweep loop (on != 0): structured loops over the field's rows with a
+ * fluid mask instead of the red/black index lists, bit-identical results; the timed
+ * CPU baseline uses it. */
+void or_set_sweep_rows(OrState* s, int on);
+/* writeResult (subWriteOutput.f90:62-72) and lastConditions (subLastConditions.f90:2-42):
+ * the reference's formatted restart file `result`. Return 0, or 1 on an I/O error or a
+ * short or malformed file. */
+int or_write_result_text(OrState* s, const char* path, double totime, int64_t ita, int64_t ita1);
+int or_read_result_text(OrState* s, const char* path, double* totime, int64_t* ita, int64_t* ita1);
 
 #ifdef __cplusplus
 }

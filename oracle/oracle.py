@@ -71,6 +71,9 @@ def lib() -> C.CDLL:
         "or_conv_coef": (_D, [_VP, C.c_int, C.c_int]),
         "or_grid1d": (_D, [_VP, C.c_int]),
         "or_set_threads": (None, [C.c_int]),
+        "or_set_sweep_rows": (None, [_VP, C.c_int]),
+        "or_write_result_text": (C.c_int, [_VP, C.c_char_p, C.c_double, C.c_int64, C.c_int64]),
+        "or_read_result_text": (C.c_int, [_VP, C.c_char_p, _D, _I64, _I64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -121,6 +124,24 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+    def set_sweep_rows(self, on: bool = True):
+        """Row form of the sweep loop (bit-identical; the timed CPU baseline uses it)."""
+        self.L.or_set_sweep_rows(self._h, 1 if on else 0)
+
+    def write_result_text(self, path, totime: float = 0.0, ita: int = 0, ita1: int = 0):
+        """writeResult: the reference's formatted `result` restart file."""
+        self._chk(self.L.or_write_result_text(self._h, str(path).encode(), float(totime), int(ita), int(ita1)),
+                  "or_write_result_text")
+
+    def read_result_text(self, path) -> tuple:
+        """lastConditions: loads u, v, w, p (ut = u ...) from `result`; returns (totime, ita, ita1)."""
+        t = np.zeros(1)
+        it = np.zeros(2, np.int64)
+        self._chk(self.L.or_read_result_text(self._h, str(path).encode(), t.ctypes.data_as(_D),
+                                             it[0:1].ctypes.data_as(_I64), it[1:2].ctypes.data_as(_I64)),
+                  "or_read_result_text")
+        return float(t[0]), int(it[0]), int(it[1])
 
     def set_solver(self, omega, eps, criterion=0, max_sweeps=1_000_000, check_every=1):
         self.L.or_set_solver(self._h, float(omega), float(eps), int(criterion), int(max_sweeps), int(check_every))

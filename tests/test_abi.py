@@ -86,3 +86,15 @@ def test_surface_mesh_files_round_trip(ib3d, built_lib, grids, tmp_path, fmt):
         path.write_text(path.read_text()[:200])
         ib3d.read_surface_mesh(path, ib3d.MESH_GMSH if fmt == "gmsh" else ib3d.MESH_GAMBIT)
     assert e.value.code == ib3d.ERR_IO
+
+
+def test_noalloc_rejects_extents_beyond_its_scratch_before_any_cuda_call(ib3d):
+    """Absurd extents (whose product would overflow int64) are rejected up front,
+    without touching a device, so this runs on a machine without a GPU."""
+    import ctypes as C
+    L = ib3d.lib()
+    dummy = C.c_void_p(1)
+    for n in ((2 ** 40, 2 ** 40, 2 ** 40), (2 ** 62, 8, 8), (200, 200, 200), (2 ** 21, 4, 4)):
+        rc = L.ib3d_pressure_solve_noalloc(*n, dummy, dummy, dummy, dummy, dummy, 0.001, dummy, 1.9, 1e-6, 10, 4,
+                                           None, None, None)
+        assert rc == ib3d.ERR_TOO_LARGE, (n, rc)

@@ -75,10 +75,14 @@ def test_poisson_cube_meets_the_record_bit_for_bit(ib3d):
     s.close()
 
 
-@pytest.mark.parametrize("name,kw", [("sphere96_fp64", {}), ("sphere96_convective", dict(outlet=1))])
+@pytest.mark.parametrize("name,kw", [("sphere96_fp64", {}), ("sphere96_convective", dict(outlet=1)),
+                                     ("sphere96_fp64", dict(precision=2))],
+                         ids=["fp64", "fp64-convective", "fp64-fast"])
 def test_200_steps_of_the_96_case_meet_the_fp64_parity_bar(ib3d, name, kw):
     """The 96x64x64 sphere at Re 100 for 200 steps, with the reference's active
-    zero-gradient outlet and with the convective (Orlanski) outlet."""
+    zero-gradient outlet and with the convective (Orlanski) outlet, and the fast
+    plain FP64 form (contracted multiply-adds, omega/diag per cell) against the same
+    record at the same bar."""
     fx = fixtures.load(name)
     s = fixtures.build_solver(ib3d, fx, **kw)
     assert _counts(s.counts) == fx["counts"].tolist()

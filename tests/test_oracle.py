@@ -518,3 +518,57 @@ def test_diffusion_is_exact_for_a_quadratic_profile(oracle_mod, grids):
     rate = (o.get_field("ut") - u)[4:-4, 4:-4, 4:-4] / cs.dt * cs.re
     assert np.max(np.abs(rate - 2.0)) < 1e-9
     o.close()
+
+
+@pytest.mark.parametrize("criterion", [0, 1])
+def test_row_form_sweeps_are_bit_identical_to_the_list_form(oracle_mod, grids, criterion):
+    """The timed CPU baseline runs the sweep loop over the field's rows with a fluid
+    mask; it must give the list form's sweep counts, drag and fields bit for bit."""
+    cs = grids.case("tiny")
+    a = oracle_mod.setup_case(cs, criterion=criterion, check_every=4)
+    b = oracle_mod.setup_case(cs, criterion=criterion, check_every=4)
+    b.set_sweep_rows(True)
+    for q in range(3):
+        sa, ca = a.step(q == 0)
+        sb, cb = b.step(q == 0)
+        assert sa["sweeps"] == sb["sweeps"]
+        assert np.array_equal(ca, cb)
+    for f in ("u", "v", "w", "p", "pc"):
+        assert np.array_equal(a.get_field(f), b.get_field(f)), f
+    a.close()
+    b.close()
+
+
+def test_result_text_round_trip_and_records_split_across_lines(oracle_mod, grids, tmp_path):
+    """writeResult/lastConditions: the formatted restart reads back exactly, also when
+    a list-directed record continues on the next line or uses commas."""
+    cs = grids.case("tiny")
+    a = oracle_mod.setup_case(cs)
+    a.step(True)
+    path = tmp_path / "result"
+    a.write_result_text(path, 0.25, 7, 3)
+    b = oracle_mod.setup_case(cs)
+    assert b.read_result_text(path) == (0.25, 7, 3)
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(a.get_field(f), b.get_field(f)), f
+    for f, g in (("ut", "u"), ("vt", "v"), ("wt", "w")):
+        assert np.array_equal(b.get_field(f), b.get_field(g)), f
+    # the same records with each one broken after its fourth value, and commas
+    lines = path.read_text().splitlines()
+    split = []
+    for ln in lines:
+        v = ln.split()
+        split.append(", ".join(v[:4]))
+        split.append("  " + " ,".join(v[4:]) + "   ignored-rest")
+    path2 = tmp_path / "result_split"
+    path2.write_text("\n".join(split) + "\n")
+    c = oracle_mod.setup_case(cs)
+    assert c.read_result_text(path2) == (0.25, 7, 3)
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(a.get_field(f), c.get_field(f)), f
+    short = tmp_path / "result_short"
+    short.write_text("\n".join(lines[:-1]) + "\n")
+    with pytest.raises(oracle_mod.OracleError):
+        c.read_result_text(short)
+    for x in (a, b, c):
+        x.close()
