@@ -519,6 +519,31 @@ def run_poisson(pkg, n: int) -> dict:
     return out
 
 
+def sweep_bench(pkg, cases=("sphere256", "sphere384"), kernels=(0, 2), steps: int = 3) -> dict:
+    """FP32 sweep kernels alone: `steps` steps of the FP32 form (previous-correction warm
+    start) on each workload with each sweep kernel; microseconds per red+black sweep
+    from the library's CUDA-event phase timers, and the algorithmic rate at 13 B per
+    cell and sweep against the measured HBM peak."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    out = {"peak_gbs": hbm}
+    for name in cases:
+        cs = workload(pkg, name)
+        for kern in kernels:
+            s = pkg.setup_case(cs, **dict(FAST, sweep_kernel=kern))
+            s.step(True)
+            s.timers_enable(True)
+            for _ in range(steps):
+                s.step(False)
+            tm = s.timers_read()
+            s.close()
+            us = 1e3 * tm["sor32_ms"] / max(tm["sweeps32"], 1)
+            gbs = BYTES_SOR32_SWEEP * cs.cells / (us * 1e-6) / 1e9
+            out[f"{name}/kernel{kern}"] = {"us_per_sweep": us, "sweeps": tm["sweeps32"], "launches": tm["launches32"],
+                                           "gbs_algorithmic": gbs, "frac": gbs / hbm}
+    return out
+
+
 def compare_fp64(pkg, cs, steps: int, net=None) -> dict:
     """The mixed-precision form (the bench's FP32 arm, learned warm start when a
     network is given) against the plain FP64 path over the same `steps` steps, both to
@@ -662,6 +687,9 @@ def main():
     ap.add_argument("--developed", type=int, default=0,
                     help="instead of the step benchmark: spin the flow up for this many steps, then time every "
                          "arm from that developed wake")
+    ap.add_argument("--sweep-bench", action="store_true",
+                    help="instead of the step benchmark: microseconds per FP32 sweep of each sweep kernel on the "
+                         "256x192x192 and 384x256x256 workloads")
     ap.add_argument("--poisson", type=int, default=0,
                     help="instead of the step benchmark: the standalone all-Neumann Poisson cube of this edge "
                          "(omega 1.85, residual 1e-8), FP64 and FP32-sweep forms")
@@ -730,6 +758,11 @@ def main():
             if mnet is not None:
                 out["speedup_learned_vs_plain_fast"] = out["fp32_learned"]["value"] / out["plain_fp64_fast"]["value"]
             print(json.dumps(out), flush=True)
+        dist.close()
+        return
+    if args.sweep_bench:
+        if dist.rank == 0:
+            print(json.dumps(sweep_bench(pkg)), flush=True)
         dist.close()
         return
     if args.poisson:

@@ -256,7 +256,7 @@ bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
          (p->precision >= IB3D_PREC_FP64 && p->precision <= IB3D_PREC_FP64_FAST) && (p->warm_start >= 0 && p->warm_start <= 2) &&
-         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel == 0 || p->sweep_kernel == 1) &&
+         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel >= 0 && p->sweep_kernel <= 2) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
          (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 && p->ramp_sweeps >= 0 &&
          (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&
@@ -503,7 +503,7 @@ void ib3d_destroy(ib3d_ctx* c) {
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
                   c->hist[0], c->hist[1], c->r_hist, c->d_norm, c->d_norm_part, c->resi[0], c->resi[1], c->resi[2],
-                  c->wdiag};
+                  c->wdiag, c->epn[0], c->epn[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);

@@ -137,6 +137,9 @@ struct ib3d_ctx {
   // colour-packed FP32 arrays of the inner solve ([0] red, [1] black); see k_sor32.cu
   float* ep[2] = {nullptr, nullptr};
   float* rp[2] = {nullptr, nullptr};
+  // second pair of colour-packed corrections for the fused sweep (sweep_kernel 2): each
+  // sweep reads ep[] and writes epn[], then the pairs swap
+  float* epn[2] = {nullptr, nullptr};
   int packed_lp = 0;
   unsigned char* cell = nullptr;
   int* ibmap = nullptr;
@@ -225,6 +228,8 @@ void launch_momentum_fast(ib3d_ctx* c, bool ab2);
 int packed_row_length(int nx);
 void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1);
 void launch_accumulate_packed(ib3d_ctx* c);
+void launch_sor32_fused(ib3d_ctx* c, float omega, float om1);
+bool fused_sweep_fits(int nx);
 // k_ib.cu
 int run_surface_norm(ib3d_ctx* c);
 int run_search(ib3d_ctx* c);

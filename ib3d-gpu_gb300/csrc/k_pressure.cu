@@ -473,7 +473,21 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   const double wi = P.omega_inner > 0.0 ? P.omega_inner : P.omega;
   const float om = (float)wi, om1 = (float)(1.0 - wi);
   const int inner = P.inner_sweeps < 1 ? 1 : P.inner_sweeps;
-  const bool packed = P.sweep_kernel == 0 && c->ep[0] != nullptr;
+  const bool fused = P.sweep_kernel == 2;
+  const bool packed = (P.sweep_kernel == 0 || fused) && c->ep[0] != nullptr;
+  if (fused) {
+    if (!packed || !fused_sweep_fits(d.nx)) {
+      c->err = "sweep_kernel 2 (fused sweep) needs an even nx of at most 1280 cells";
+      return IB3D_ERR_ARG;
+    }
+    if (!c->epn[0]) {
+      const size_t np = (size_t)c->packed_lp * (size_t)d.NY2 * (size_t)d.NZ2;
+      for (int q = 0; q < 2; ++q) {
+        if (cudaMalloc(&c->epn[q], np * sizeof(float)) != cudaSuccess) return IB3D_ERR_MEMORY;
+        IB3D_CUDA(c, cudaMemsetAsync(c->epn[q], 0, np * sizeof(float), c->st));
+      }
+    }
+  }
   int rc = reset_ctl(c);
   if (rc) return rc;
   if (!packed) IB3D_CUDA(c, cudaMemsetAsync(c->e32, 0, sizeof(float) * (size_t)d.n3, c->st));
@@ -514,8 +528,8 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     prev_res = res;
     {
       PhaseScope ps(c, PH_SOR32);
-      c->launches += 2 * batch;
-      c->t_launches32 += 2 * batch;
+      c->launches += fused ? batch : 2 * batch;
+      c->t_launches32 += fused ? batch : 2 * batch;
       for (int q = 0; q < batch; ++q) {
         // the solve's first sweeps run at relaxation 1 (smooth_sweeps: Gauss-Seidel damps the
         // high-frequency error that the over-relaxed sweeps barely touch), the next
@@ -527,7 +541,9 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
           w = (float)wr;
           w1 = (float)(1.0 - wr);
         }
-        if (packed) {
+        if (fused) {
+          launch_sor32_fused(c, w, w1);
+        } else if (packed) {
           launch_sor32_packed(c, 0, w, w1);
           launch_sor32_packed(c, 1, w, w1);
         } else {

@@ -337,6 +337,43 @@ void or_no_body(OrState* s) {
   s->nelp = (int64_t*)calloc(1, sizeof(int64_t));
 }
 
+/* The tagging test of one cell (subSearch.f90:166-247, and the same lines of
+ * selectiveRetagging, :361-435): the nearest surface centroid of the cell centre
+ * (dsqrt of the squared distances in y, x, z order; strict '<', so the first minimum
+ * wins), then the signs of the eight corner distances to that element's plane
+ * against -1e-16: all <= solid (1), all > fluid (0), else IB (2). */
+static void tag_cell(OrState* s, int64_t i, int64_t j, int64_t k) {
+  const double thr = -1e-16;
+  double minDis = 1e14;
+  int64_t nel = 0;
+  const double n1x = s->xp[i], n1y = s->yp[j], n1z = s->zp[k];
+  const double n2x = s->x1[i], n3x = s->x1[i + 1];
+  const double n2y = s->y1[j], n3y = s->y1[j + 1];
+  const double n2z = s->z1[k], n3z = s->z1[k + 1];
+  for (int64_t m = 1; m <= s->nelems; ++m) {          /* :187-196 */
+    double dis = sqrt((SQ(n1y - s->ycent[m]) + SQ(n1x - s->xcent[m])) + SQ(n1z - s->zcent[m]));
+    if (dis < minDis) { minDis = dis; nel = m; }
+  }
+  F3(s->minElemcell, i, j, k) = nel;                   /* :198 */
+  double d[8];
+  d[0] = corner_dot(s, nel, n2x, n2y, n2z);            /* n2dotn :204 */
+  d[1] = corner_dot(s, nel, n2x, n3y, n2z);            /* n3dotn :208 */
+  d[2] = corner_dot(s, nel, n3x, n2y, n2z);            /* n4dotn :212 */
+  d[3] = corner_dot(s, nel, n3x, n3y, n2z);            /* n5dotn :216 */
+  d[4] = corner_dot(s, nel, n2x, n2y, n3z);            /* n6dotn :220 */
+  d[5] = corner_dot(s, nel, n2x, n3y, n3z);            /* n7dotn :224 */
+  d[6] = corner_dot(s, nel, n3x, n2y, n3z);            /* n8dotn :228 */
+  d[7] = corner_dot(s, nel, n3x, n3y, n3z);            /* n9dotn :232 */
+  int all_in = 1, all_out = 1;
+  for (int q = 0; q < 8; ++q) {
+    if (!(d[q] <= thr)) all_in = 0;
+    if (!(d[q] > thr)) all_out = 0;
+  }
+  F3(s->cell, i, j, k) = all_in ? 1 : (all_out ? 0 : 2);   /* :238-247 */
+}
+
+static void norm_distance(OrState* s);
+
 /* tagging (subSearch.f90:134-321), cellCount (515-596), computeNormDistance (599-678). */
 int or_search(OrState* s, const int64_t box[6]) {
   const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
@@ -345,39 +382,51 @@ int or_search(OrState* s, const int64_t box[6]) {
   memset(s->minElemcell, 0, (size_t)n3 * sizeof(int64_t));  /* :151 */
   if (box[0] < 1 || box[1] > nx + 2 || box[2] < 1 || box[3] > ny + 2 || box[4] < 1 || box[5] > nz + 2)
     return -2;
-  const double thr = -1e-16;
 #pragma omp parallel for collapse(2) schedule(static)
   for (int64_t k = box[4]; k <= box[5]; ++k)
     for (int64_t j = box[2]; j <= box[3]; ++j)
-      for (int64_t i = box[0]; i <= box[1]; ++i) {
-        double minDis = 1e14;
-        int64_t nel = 0;
-        const double n1x = s->xp[i], n1y = s->yp[j], n1z = s->zp[k];
-        const double n2x = s->x1[i], n3x = s->x1[i + 1];
-        const double n2y = s->y1[j], n3y = s->y1[j + 1];
-        const double n2z = s->z1[k], n3z = s->z1[k + 1];
-        for (int64_t m = 1; m <= s->nelems; ++m) {          /* :187-196 */
-          double dis = sqrt((SQ(n1y - s->ycent[m]) + SQ(n1x - s->xcent[m])) + SQ(n1z - s->zcent[m]));
-          if (dis < minDis) { minDis = dis; nel = m; }
-        }
-        F3(s->minElemcell, i, j, k) = nel;                   /* :198 */
-        double d[8];
-        d[0] = corner_dot(s, nel, n2x, n2y, n2z);            /* n2dotn :204 */
-        d[1] = corner_dot(s, nel, n2x, n3y, n2z);            /* n3dotn :208 */
-        d[2] = corner_dot(s, nel, n3x, n2y, n2z);            /* n4dotn :212 */
-        d[3] = corner_dot(s, nel, n3x, n3y, n2z);            /* n5dotn :216 */
-        d[4] = corner_dot(s, nel, n2x, n2y, n3z);            /* n6dotn :220 */
-        d[5] = corner_dot(s, nel, n2x, n3y, n3z);            /* n7dotn :224 */
-        d[6] = corner_dot(s, nel, n3x, n2y, n3z);            /* n8dotn :228 */
-        d[7] = corner_dot(s, nel, n3x, n3y, n3z);            /* n9dotn :232 */
-        int all_in = 1, all_out = 1;
-        for (int q = 0; q < 8; ++q) {
-          if (!(d[q] <= thr)) all_in = 0;
-          if (!(d[q] > thr)) all_out = 0;
-        }
-        F3(s->cell, i, j, k) = all_in ? 1 : (all_out ? 0 : 2);   /* :238-247 */
-      }
+      for (int64_t i = box[0]; i <= box[1]; ++i) tag_cell(s, i, j, k);
   cell_count(s);
+  norm_distance(s);
+  return 0;
+}
+
+/* selectiveRetagging (subSearch.f90:327-512): minElemcell = 0 (:339), then the
+ * tagging test on the 6x6x6 neighbourhood i1-2..i1+3, j1-2..j1+3, k1-2..k1+3 of every
+ * IB cell (i1, j1, k1) of the current list (:355-435); every other cell keeps its
+ * flag. Neighbourhoods overlap, but the test depends on the cell alone, so the order
+ * does not matter. The neighbourhood is clipped to the interior cells (a body kept
+ * three cells from the walls never reaches the clip). Then cellCount (:515-596; the
+ * reference recounts at :445-463) and computeNormDistance (:599-678), as after
+ * tagging. Returns 0, or -1 when no IB cell exists to start from. */
+int or_selective_retag(OrState* s) {
+  const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
+  const int64_t n3 = NX2 * NY2 * (nz + 2);
+  const int64_t nb = s->nib;
+  if (nb < 1) return -1;
+  memset(s->minElemcell, 0, (size_t)n3 * sizeof(int64_t));
+  /* the neighbourhoods' cells, each once, so that the OpenMP loop writes each cell once */
+  unsigned char* mark = (unsigned char*)calloc((size_t)n3, 1);
+  for (int64_t nn = 1; nn <= nb; ++nn) {
+    const int64_t i1 = L(s->ib, nb, nn, 1), j1 = L(s->ib, nb, nn, 2), k1 = L(s->ib, nb, nn, 3);
+    for (int64_t k = k1 - 2; k <= k1 + 3; ++k)
+      for (int64_t j = j1 - 2; j <= j1 + 3; ++j)
+        for (int64_t i = i1 - 2; i <= i1 + 3; ++i)
+          if (i >= 2 && i <= nx + 1 && j >= 2 && j <= ny + 1 && k >= 2 && k <= nz + 1) F3(mark, i, j, k) = 1;
+  }
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
+  for (int64_t k = 2; k <= nz + 1; ++k)
+    for (int64_t j = 2; j <= ny + 1; ++j)
+      for (int64_t i = 2; i <= nx + 1; ++i)
+        if (F3(mark, i, j, k)) tag_cell(s, i, j, k);
+  free(mark);
+  cell_count(s);
+  norm_distance(s);
+  return 0;
+}
+
+/* computeNormDistance (subSearch.f90:599-678) over the IB list cellCount built. */
+static void norm_distance(OrState* s) {
   const int64_t nb = s->nib;
   /* computeNormDistance (subSearch.f90:621-672). */
   for (int q = 0; q < 7; ++q) { free(s->nd[q]); s->nd[q] = alloc1(nb); }
@@ -399,7 +448,6 @@ int or_search(OrState* s, const int64_t box[6]) {
     s->nd[6][n] = corner_dot(s, m, n1x, n1y, n3z);   /* w2NormDis :669 */
   }
   s->have_scache = 0;
-  return 0;
 }
 
 /* initialConditions (subInitialConditions.f90:2-48). */

@@ -61,6 +61,11 @@ int or_move_body_free(OrState* s, double fx, double fy, double fz, double vel[3]
  * box = {i_start, i_end, j_start, j_end, k_start, k_end} (1-based, inclusive). */
 int or_search(OrState* s, const int64_t box[6]);
 
+/* selectiveRetagging (subSearch.f90:327-512): re-tags the 6x6x6 neighbourhood of every
+ * IB cell of the current list (after a small move of the body), then cellCount and
+ * computeNormDistance. Returns 0, or -1 with no IB cells to start from. */
+int or_selective_retag(OrState* s);
+
 /* No body at all: every interior cell fluid, lists built as cellCount does. */
 void or_no_body(OrState* s);
 

@@ -39,6 +39,7 @@ def lib() -> C.CDLL:
         "or_set_mesh": (C.c_int, [_VP, C.c_int64, _D, _D, _D, C.c_int64, _I64, _I64, _I64, C.c_double, C.c_double,
                                   C.c_double, C.c_int64]),
         "or_search": (C.c_int, [_VP, _I64]),
+        "or_selective_retag": (C.c_int, [_VP]),
         "or_move_body": (C.c_int, [_VP] + [C.c_double] * 6),
         "or_initial_conditions": (None, [_VP]),
         "or_coefficient_matrix": (None, [_VP]),
@@ -178,6 +179,14 @@ class Oracle:
     def search(self, box) -> dict:
         b = np.asarray(box, dtype=np.int64)
         self._chk(self.L.or_search(self._h, b.ctypes.data_as(_I64)), "or_search")
+        c = np.zeros(5, dtype=np.int64)
+        self.L.or_counts(self._h, c.ctypes.data_as(_I64))
+        self.counts = dict(zip(("fluid", "solid", "ib", "red", "black"), (int(v) for v in c)))
+        return self.counts
+
+    def selective_retag(self) -> dict:
+        """selectiveRetagging: re-tag the 6^3 neighbourhoods of the current IB cells."""
+        self._chk(self.L.or_selective_retag(self._h), "or_selective_retag")
         c = np.zeros(5, dtype=np.int64)
         self.L.or_counts(self._h, c.ctypes.data_as(_I64))
         self.counts = dict(zip(("fluid", "solid", "ib", "red", "black"), (int(v) for v in c)))

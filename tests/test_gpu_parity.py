@@ -200,14 +200,15 @@ def test_mixed_precision_matches_fp64_drag(ib3d, grids):
     s64.close(); s32.close()
 
 
-@pytest.mark.parametrize("name", ["tiny", "small"])
-def test_packed_fp32_sweep_matches_padded_layout(ib3d, grids, name):
-    """The FP32 sweep on colour-packed arrays performs the same red-then-black
+@pytest.mark.parametrize("name,kernel", [("tiny", 0), ("small", 0), ("tiny", 2), ("small", 2)])
+def test_packed_fp32_sweep_matches_padded_layout(ib3d, grids, name, kernel):
+    """The FP32 sweep on colour-packed arrays (two colour passes, kernel 0, or one
+    fused z-wavefront launch per sweep, kernel 2) performs the same red-then-black
     update with the same FP32 operation order as the sweep on the padded field
     layout, so whole mixed-precision steps agree bit for bit."""
     cs = grids.case(name)
     common = dict(precision=ib3d.PREC_FP32DC, criterion=ib3d.CRIT_RESIDUAL, eps=1e-6, inner_sweeps=7)
-    a = ib3d.setup_case(cs, sweep_kernel=0, **common)
+    a = ib3d.setup_case(cs, sweep_kernel=kernel, **common)
     b = ib3d.setup_case(cs, sweep_kernel=1, **common)
     for step in range(1, 4):
         sa, ca = a.step(step == 1)

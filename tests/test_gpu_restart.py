@@ -81,3 +81,43 @@ def test_restart_errors(ib3d, grids, tmp_path):
     assert e.value.code == ib3d.ERR_IO
     a.close()
     other.close()
+
+
+def test_library_result_file_restarts_the_oracle_bit_exact(ib3d, grids, oracle_mod, tmp_path):
+    """The library writes the reference's `result` file after 3 steps; the oracle's
+    own restatement of lastConditions (subLastConditions.f90:2-42) reads it, and both
+    continue for 3 steps: sweep counts, drag/lift and fields must be bit-identical.
+    The reverse direction too: the library reads the oracle's writeResult file
+    (subWriteOutput.f90:62-72), including records split across lines."""
+    cs = grids.case("tiny")
+    s = ib3d.setup_case(cs)
+    for step in range(1, 4):
+        s.step(step == 1)
+    path = tmp_path / "result"
+    s.write_restart(path, totime=3 * cs.dt, ita=3, ita1=3, text=True)
+    o = oracle_mod.setup_case(cs)
+    assert o.read_result_text(path) == (3 * cs.dt, 3, 3)
+    for f in ("u", "v", "w", "p", "ut", "vt", "wt"):
+        assert np.array_equal(o.get_field(f), s.get_field(f)), f
+    for step in range(3):   # both re-bracket the drag probes on the first step after the restart
+        ss, cs_ = s.step(step == 0)
+        so, co = o.step(step == 0)
+        assert ss["sweeps"] == so["sweeps"], step
+        assert np.array_equal(cs_, co), step
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(o.get_field(f), s.get_field(f)), f
+    # the oracle's file, each record broken over two lines, read by the library
+    path2 = tmp_path / "result_oracle"
+    o.write_result_text(path2, 6 * cs.dt, 6, 6)
+    lines = path2.read_text().splitlines()
+    split = []
+    for ln in lines:
+        v = ln.split()
+        split += [" ".join(v[:3]), ", ".join(v[3:])]
+    path2.write_text("\n".join(split) + "\n")
+    b = ib3d.setup_case(cs)
+    assert b.read_restart(path2, text=True) == (6 * cs.dt, 6, 6)
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(b.get_field(f), o.get_field(f)), f
+    for x in (s, o, b):
+        x.close()

@@ -572,3 +572,28 @@ def test_result_text_round_trip_and_records_split_across_lines(oracle_mod, grids
         c.read_result_text(short)
     for x in (a, b, c):
         x.close()
+
+
+def test_selective_retagging_matches_the_full_search_after_small_moves(oracle_mod, grids):
+    """selectiveRetagging re-tags only the 6^3 neighbourhoods of the IB cells. For a
+    body that moves less than a cell per step, every cell whose flag changes lies in
+    such a neighbourhood, so the flags, IB list, nearest elements and normal
+    distances equal those of a full search of the box."""
+    cs = grids.case("tiny")
+    a = oracle_mod.setup_case(cs)
+    b = oracle_mod.setup_case(cs)
+    h = float(np.min(np.diff(cs.x)))
+    y = 0.0
+    for q in range(6):
+        dy = 0.3 * h * (1 if q % 3 else -1)
+        y += dy
+        a.move_body(0.0, dy, 0.0)
+        b.move_body(0.0, dy, 0.0)
+        ca = a.search(grids.body_box(cs, (0.0, y, 0.0)))
+        cb = b.selective_retag()
+        assert ca == cb, q
+        ga, gb = a.get_search(), b.get_search()
+        for key in ("cell", "ib", "nelp", "normdis"):
+            assert np.array_equal(ga[key], gb[key]), (q, key)
+    a.close()
+    b.close()
