@@ -579,10 +579,11 @@ def compare_fp64(pkg, cs, steps: int, net=None) -> dict:
 
 
 def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, freq: float = 0.2, net=None,
-               perturb: float = 0.0, seed: int = 0, capture=None) -> dict:
+               perturb: float = 0.0, seed: int = 0, capture=None, selective: bool = True) -> dict:
     """The body oscillates as y(t) = amp sin(2 pi freq t): before every step the nodes
-    move (ib3d_move_body, surface velocity y'(t)), the search re-tags a box around
-    the new position, then the step runs. Timed with CUDA events on the library
+    move (ib3d_move_body, surface velocity y'(t)), then selectiveRetagging re-tags the
+    neighbourhoods of the IB cells (selective=False: the search re-tags a whole box
+    around the new position), then the step runs. Timed with CUDA events on the library
     stream around the timed steps (move, search and step together). With `net` the
     solve starts from the network's guess; `perturb` adds a seeded relative
     perturbation to the initial u; `capture` = (network, patches) captures training
@@ -614,7 +615,10 @@ def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, f
         s.move_body(0.0, yn - y, 0.0, 0.0, amp * w * math.cos(w * t), 0.0)
         y = yn
         t0 = time.perf_counter()
-        s.search(pkg.grids.body_box(cs, (0.0, y, 0.0)))
+        if selective:
+            s.selective_retag()
+        else:
+            s.search(pkg.grids.body_box(cs, (0.0, y, 0.0)))
         if n > warmup:
             t_search += time.perf_counter() - t0
         st, coef = s.step(n == 1)
@@ -628,6 +632,7 @@ def run_moving(pkg, cs, mode: dict, warmup: int, steps: int, amp: float = 0.2, f
     s.close()
     return {"value": steps / sec, "unit": "steps/s", "ms_per_step": 1e3 * sec / steps,
             "sweeps_per_step": sum(sweeps) / len(sweeps), "search_ms_per_step": 1e3 * t_search / steps,
+            "search": "selectiveRetagging" if selective else "tagging of the whole box",
             "drag_lift": list(map(float, coef)), "y_end": y}
 
 
@@ -748,7 +753,8 @@ def main():
             mcs = workload(pkg, args.case if args.case != "sphere256" else "sphere384")
             out = {"workload": f"{mcs.name} {mcs.shape[0]}x{mcs.shape[1]}x{mcs.shape[2]}, Re {mcs.re:g}, moving sphere "
                                "y = 0.2 sin(2 pi 0.2 t), search every step, residual <= 1e-6",
-                   "fp32": run_moving(pkg, mcs, FAST, warmup, args.steps)}
+                   "fp32": run_moving(pkg, mcs, FAST, warmup, args.steps),
+                   "fp32_full_search": run_moving(pkg, mcs, FAST, warmup, args.steps, selective=False)}
             mnet = load_net(pkg, args.weights, args.coarsen)
             if mnet is not None:
                 out["fp32_learned"] = run_moving(pkg, mcs, FAST, warmup, args.steps, net=mnet)

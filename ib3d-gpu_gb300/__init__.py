@@ -107,6 +107,7 @@ def lib() -> C.CDLL:
         "ib3d_set_mesh": (C.c_int, [_VP, C.c_int64, _D, _D, _D, C.c_int64, _I64, _I64, _I64, C.c_double,
                                     C.c_double, C.c_double, C.c_int64]),
         "ib3d_search": (C.c_int, [_VP, _I64, _I64]),
+        "ib3d_selective_retag": (C.c_int, [_VP, _I64]),
         "ib3d_move_body": (C.c_int, [_VP] + [C.c_double] * 6),
         "ib3d_move_body_free": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _D]),
         "ib3d_read_surface_mesh": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, _I64, _D, _D, _D, _I64, _I64, _I64,
@@ -246,6 +247,14 @@ class Solver:
         b = np.asarray(box, dtype=np.int64)
         counts = np.zeros(5, dtype=np.int64)
         self._check(self.L.ib3d_search(self._h, _ip(b), _ip(counts)), "ib3d_search")
+        self.counts = dict(zip(("fluid", "solid", "ib", "red", "black"), (int(v) for v in counts)))
+        return self.counts
+
+    def selective_retag(self) -> dict:
+        """selectiveRetagging: re-tag the 6^3 neighbourhoods of the current IB cells
+        (after move_body, in place of search)."""
+        counts = np.zeros(5, dtype=np.int64)
+        self._check(self.L.ib3d_selective_retag(self._h, _ip(counts)), "ib3d_selective_retag")
         self.counts = dict(zip(("fluid", "solid", "ib", "red", "black"), (int(v) for v in counts)))
         return self.counts
 

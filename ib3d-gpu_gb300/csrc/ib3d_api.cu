@@ -503,7 +503,7 @@ void ib3d_destroy(ib3d_ctx* c) {
                   c->e32, c->r32, c->ep[0], c->ep[1], c->rp[0], c->rp[1], c->cell, c->ibmap, c->ctl, c->d_nodes, c->d_tri, c->d_surf, c->d_iblist,
                   c->d_nelp, c->d_nd, c->d_minel, c->d_scache, c->d_contrib, c->d_coef, c->d_flag, c->d_scan,
                   c->hist[0], c->hist[1], c->r_hist, c->d_norm, c->d_norm_part, c->resi[0], c->resi[1], c->resi[2],
-                  c->wdiag, c->epn[0], c->epn[1]};
+                  c->wdiag, c->epn[0], c->epn[1], c->d_retag_mask, c->d_retag_list};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -574,6 +574,7 @@ int ib3d_set_mesh(ib3d_ctx* c, int64_t nnodes, const double* xn, const double* y
   for (double x : cosv)
     if (!std::isfinite(x)) return fail(c, IB3D_ERR_MESH, "ib3d_set_mesh: degenerate triangle (zero area)");
   c->searched = false;
+  c->retag_ok = false;
   c->have_scache = false;
   return IB3D_OK;
 }
@@ -606,9 +607,25 @@ int ib3d_search(ib3d_ctx* c, const int64_t box[6], int64_t counts[5]) {
     if (box[2 * a] < 1 || box[2 * a + 1] > hi[a] || box[2 * a] > box[2 * a + 1])
       return fail(c, IB3D_ERR_ARG, "ib3d_search: search box outside the padded grid");
   for (int q = 0; q < 6; ++q) c->box[q] = box[q];
+  c->retag_ok = false;
   int rc = run_search(c);
   if (rc) return rc;
   c->searched = true;
+  c->retag_ok = true;
+  if (counts)
+    for (int q = 0; q < 5; ++q) counts[q] = c->counts[q];
+  return IB3D_OK;
+}
+
+int ib3d_selective_retag(ib3d_ctx* c, int64_t counts[5]) {
+  if (!c) return IB3D_ERR_ARG;
+  if (!c->retag_ok || c->nib < 1)
+    return fail(c, IB3D_ERR_ARG, "ib3d_selective_retag: needs the IB cells of an earlier search of this mesh");
+  c->retag_ok = false;
+  int rc = run_selective_retag(c);
+  if (rc) return rc;
+  c->searched = true;
+  c->retag_ok = c->nib > 0;
   if (counts)
     for (int q = 0; q < 5; ++q) counts[q] = c->counts[q];
   return IB3D_OK;

@@ -156,6 +156,11 @@ struct ib3d_ctx {
 
   // search results
   bool searched = false;
+  bool retag_ok = false;            // an IB list of this mesh exists (ib3d_selective_retag may run)
+  unsigned char* d_retag_mask = nullptr;  // selectiveRetagging: neighbourhood mask over their bounding box
+  int* d_retag_list = nullptr;            // and the marked cells (i, j, k blocks)
+  size_t retag_cap = 0;
+  long long retagged = 0;                 // cells tagged by the last selective retag
   long long counts[5] = {0, 0, 0, 0, 0};
   int nib = 0;
   int* d_iblist = nullptr;    // 3*nib (i block, j block, k block), 1-based
@@ -233,6 +238,7 @@ bool fused_sweep_fits(int nx);
 // k_ib.cu
 int run_surface_norm(ib3d_ctx* c);
 int run_search(ib3d_ctx* c);
+int run_selective_retag(ib3d_ctx* c);
 int run_velocity_forcing(ib3d_ctx* c);
 int run_pressure_forcing(ib3d_ctx* c);
 int run_stress(ib3d_ctx* c, int first, double coef[4]);

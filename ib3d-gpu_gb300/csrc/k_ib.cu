@@ -161,22 +161,32 @@ __device__ __forceinline__ double corner_dot(const double* surf, int ne, int e, 
 // element whose squared distance is not below the current best's squared distance
 // cannot have a strictly smaller rounded root, so the root is only taken for
 // candidates that improve the squared distance: the same argmin, bit for bit.
-// Centroids are staged through shared memory in tiles.
+// Centroids are staged through shared memory in tiles. The cells tagged are the
+// box's (list == nullptr), or the nlist cells of a list inside the box (the
+// neighbourhoods of selectiveRetagging); minel is indexed by the cell's position in
+// the box either way.
 constexpr int kTagTile = 512;
 __global__ void __launch_bounds__(kBlock) k_tagging(Dims d, Grid1D g, const double* __restrict__ surf, int ne,
                                                     int bi0, int bj0, int bk0, int bni, int bnj, int bnk,
+                                                    const int* __restrict__ list, int nlist,
                                                     unsigned char* __restrict__ cell, int* __restrict__ minel) {
   __shared__ double sx[kTagTile], sy[kTagTile], sz[kTagTile];
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned nbox = (unsigned)bni * (unsigned)bnj * (unsigned)bnk;
-  const bool active = tid < nbox;
+  const unsigned ncell = list ? (unsigned)nlist : (unsigned)bni * (unsigned)bnj * (unsigned)bnk;
+  const bool active = tid < ncell;
   int i = 0, j = 0, k = 0;
   double n1x = 0, n1y = 0, n1z = 0;
   if (active) {
-    i = bi0 + (int)(tid % (unsigned)bni);
-    const unsigned t = tid / (unsigned)bni;
-    j = bj0 + (int)(t % (unsigned)bnj);
-    k = bk0 + (int)(t / (unsigned)bnj);
+    if (list) {
+      i = list[tid];
+      j = list[nlist + tid];
+      k = list[2 * nlist + tid];
+    } else {
+      i = bi0 + (int)(tid % (unsigned)bni);
+      const unsigned t = tid / (unsigned)bni;
+      j = bj0 + (int)(t % (unsigned)bnj);
+      k = bk0 + (int)(t / (unsigned)bnj);
+    }
     n1x = g.xp[i]; n1y = g.yp[j]; n1z = g.zp[k];
   }
   double best = 1e14, best2 = 1e300;
@@ -220,7 +230,82 @@ __global__ void __launch_bounds__(kBlock) k_tagging(Dims d, Grid1D g, const doub
     if (!(dd[q] > thr)) all_out = false;
   }
   cell[d.at(i, j, k)] = all_in ? 1 : (all_out ? 0 : 2);
-  minel[tid] = nel;
+  minel[(i - bi0) + bni * ((j - bj0) + bnj * (k - bk0))] = nel;
+}
+
+// Bounding box of the IB list: {min i, max i, min j, max j, min k, max k}, out[] set
+// to {INT_MAX, INT_MIN, ...} before the launch.
+__global__ void k_ib_bounds(const int* __restrict__ iblist, int nib, int* __restrict__ out) {
+  int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nib; n += gridDim.x * blockDim.x)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int v = iblist[a * nib + n];
+      lo[a] = min(lo[a], v);
+      hi[a] = max(hi[a], v);
+    }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = min(lo[a], __shfl_down_sync(0xffffffffu, lo[a], o));
+      hi[a] = max(hi[a], __shfl_down_sync(0xffffffffu, hi[a], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&out[2 * a], lo[a]);
+      atomicMax(&out[2 * a + 1], hi[a]);
+    }
+  }
+}
+
+// selectiveRetagging's neighbourhoods (subSearch.f90:355-358): cells i1-2..i1+3,
+// j1-2..j1+3, k1-2..k1+3 of every IB cell (i1,j1,k1), clipped to the box (the
+// neighbourhoods' bounding box clipped to the interior), marked in a box-shaped mask.
+// Overlapping neighbourhoods write the same value.
+__global__ void k_mark_neighbourhoods(const int* __restrict__ iblist, int nib, int bi0, int bj0, int bk0, int bni,
+                                      int bnj, int bnk, unsigned char* __restrict__ mask) {
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (unsigned)nib * 216u) return;
+  const int n = (int)(tid / 216u), o = (int)(tid % 216u);
+  const int i = iblist[n] - 2 + o % 6, j = iblist[nib + n] - 2 + (o / 6) % 6, k = iblist[2 * nib + n] - 2 + o / 36;
+  const int li = i - bi0, lj = j - bj0, lk = k - bk0;
+  if (li >= 0 && li < bni && lj >= 0 && lj < bnj && lk >= 0 && lk < bnk) mask[li + bni * (lj + bnj * lk)] = 1;
+}
+
+// Compaction of the marked cells of a box-shaped mask into a list (i block, j block,
+// k block); same three passes as the IB compaction below.
+__global__ void k_mask_blockcount(const unsigned char* __restrict__ mask, unsigned nbox, long long* bcount) {
+  __shared__ int s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = t < nbox && mask[t];
+  const unsigned bal = __ballot_sync(0xffffffffu, f);
+  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&s, __popc(bal));
+  __syncthreads();
+  if (threadIdx.x == 0) bcount[blockIdx.x] = s;
+}
+__global__ void k_mask_scatter(const unsigned char* __restrict__ mask, unsigned nbox, int bi0, int bj0, int bk0,
+                               int bni, int bnj, const long long* __restrict__ boff, int nlist,
+                               int* __restrict__ list) {
+  __shared__ int wsum[kBlock / 32];
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = t < nbox && mask[t];
+  const unsigned bal = __ballot_sync(0xffffffffu, f);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) wsum[wid] = __popc(bal);
+  __syncthreads();
+  int before = 0;
+  for (int q = 0; q < wid; ++q) before += wsum[q];
+  before += __popc(bal & ((1u << lane) - 1u));
+  if (f) {
+    const long long n = boff[blockIdx.x] + before;
+    if (n < nlist) {
+      list[n] = bi0 + (int)(t % (unsigned)bni);
+      const unsigned r = t / (unsigned)bni;
+      list[nlist + n] = bj0 + (int)(r % (unsigned)bnj);
+      list[2 * nlist + n] = bk0 + (int)(r / (unsigned)bnj);
+    }
+  }
 }
 
 // Cell counts over the interior (subSearch.f90:259-270) and the red/black split of
@@ -709,6 +794,20 @@ void free_ib(ib3d_ctx* c) {
   free_sched(c->fp);
 }
 
+namespace {
+// Scratch of at least `n` long longs in c->d_scan (counts at 0..7, block offsets from 8).
+int ensure_scan(ib3d_ctx* c, size_t n) {
+  if (n + 9 > c->scan_cap) {
+    cudaFree(c->d_scan);
+    c->d_scan = nullptr;
+    c->scan_cap = n + 64;
+    IB3D_CUDA(c, cudaMalloc(&c->d_scan, sizeof(long long) * c->scan_cap));
+  }
+  return IB3D_OK;
+}
+int finish_search(ib3d_ctx* c, int bi0, int bj0, int bk0, int bni, int bnj, int bnk);
+}  // namespace
+
 int run_search(ib3d_ctx* c) {
   const Dims& d = c->d;
   const int bi0 = (int)c->box[0], bj0 = (int)c->box[2], bk0 = (int)c->box[4];
@@ -718,13 +817,80 @@ int run_search(ib3d_ctx* c) {
   const int ne = (int)c->nelems;
   // fresh flags and maps
   IB3D_CUDA(c, cudaMemsetAsync(c->cell, 0, (size_t)d.n3, c->st));
-  IB3D_CUDA(c, cudaMemsetAsync(c->ibmap, 0xff, sizeof(int) * (size_t)d.n3, c->st));
   cudaFree(c->d_minel);
   c->d_minel = nullptr;
   IB3D_CUDA(c, cudaMalloc(&c->d_minel, sizeof(int) * (size_t)nbox));
-  k_tagging<<<nblk(nbox), kBlock, 0, c->st>>>(d, c->g, c->d_surf, ne, bi0, bj0, bk0, bni, bnj, bnk, c->cell,
-                                               c->d_minel);
+  k_tagging<<<nblk(nbox), kBlock, 0, c->st>>>(d, c->g, c->d_surf, ne, bi0, bj0, bk0, bni, bnj, bnk, nullptr, 0,
+                                               c->cell, c->d_minel);
   IB3D_CUDA(c, cudaGetLastError());
+  return finish_search(c, bi0, bj0, bk0, bni, bnj, bnk);
+}
+
+// selectiveRetagging (subSearch.f90:327-512): the tagging test on the 6x6x6
+// neighbourhood of every cell of the current IB list, every other cell keeping its
+// flag; then the counts, the IB list, the normal distances and the ghost-point
+// schedules as after a full search. The neighbourhoods' cells are marked in a mask
+// over their bounding box (clipped to the interior), compacted into a list, and only
+// those are tagged.
+int run_selective_retag(ib3d_ctx* c) {
+  const Dims& d = c->d;
+  const int nib = c->nib, ne = (int)c->nelems;
+  int* dbound = reinterpret_cast<int*>(c->d_scan);
+  const int init[6] = {0x7fffffff, -0x7fffffff, 0x7fffffff, -0x7fffffff, 0x7fffffff, -0x7fffffff};
+  IB3D_CUDA(c, cudaMemcpyAsync(dbound, init, sizeof(init), cudaMemcpyHostToDevice, c->st));
+  k_ib_bounds<<<std::min(nblk(nib), 64u), kBlock, 0, c->st>>>(c->d_iblist, nib, dbound);
+  int hb[6];
+  IB3D_CUDA(c, cudaMemcpyAsync(hb, dbound, sizeof(hb), cudaMemcpyDeviceToHost, c->st));
+  IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  const int bi0 = std::max(hb[0] - 2, 2), bi1 = std::min(hb[1] + 3, d.nx + 1);
+  const int bj0 = std::max(hb[2] - 2, 2), bj1 = std::min(hb[3] + 3, d.ny + 1);
+  const int bk0 = std::max(hb[4] - 2, 2), bk1 = std::min(hb[5] + 3, d.nz + 1);
+  const int bni = bi1 - bi0 + 1, bnj = bj1 - bj0 + 1, bnk = bk1 - bk0 + 1;
+  const unsigned nbox = (unsigned)bni * bnj * bnk;
+  cudaFree(c->d_minel);
+  c->d_minel = nullptr;
+  IB3D_CUDA(c, cudaMalloc(&c->d_minel, sizeof(int) * (size_t)nbox));
+  IB3D_CUDA(c, cudaMemsetAsync(c->d_minel, 0, sizeof(int) * (size_t)nbox, c->st));
+  if ((size_t)nbox > c->retag_cap) {
+    cudaFree(c->d_retag_mask);
+    cudaFree(c->d_retag_list);
+    c->d_retag_mask = nullptr;
+    c->d_retag_list = nullptr;
+    c->retag_cap = (size_t)nbox + (size_t)nbox / 4;
+    IB3D_CUDA(c, cudaMalloc(&c->d_retag_mask, c->retag_cap));
+    IB3D_CUDA(c, cudaMalloc(&c->d_retag_list, 3 * sizeof(int) * c->retag_cap));
+  }
+  IB3D_CUDA(c, cudaMemsetAsync(c->d_retag_mask, 0, nbox, c->st));
+  k_mark_neighbourhoods<<<nblk(216ll * nib), kBlock, 0, c->st>>>(c->d_iblist, nib, bi0, bj0, bk0, bni, bnj, bnk,
+                                                                  c->d_retag_mask);
+  const unsigned nb = nblk(nbox);
+  if (int rc = ensure_scan(c, nb)) return rc;
+  long long* boff = c->d_scan + 8;
+  k_mask_blockcount<<<nb, kBlock, 0, c->st>>>(c->d_retag_mask, nbox, boff);
+  k_exclusive_scan<<<1, 1024, 0, c->st>>>(boff, (int)nb, c->d_scan);
+  long long nlist = 0;
+  IB3D_CUDA(c, cudaMemcpyAsync(&nlist, c->d_scan, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+  IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  // the list is sized for the whole box: the three index blocks start nlist apart
+  k_mask_scatter<<<nb, kBlock, 0, c->st>>>(c->d_retag_mask, nbox, bi0, bj0, bk0, bni, bnj, boff, (int)nlist,
+                                           c->d_retag_list);
+  if (nlist > 0)
+    k_tagging<<<nblk(nlist), kBlock, 0, c->st>>>(d, c->g, c->d_surf, ne, bi0, bj0, bk0, bni, bnj, bnk,
+                                                 c->d_retag_list, (int)nlist, c->cell, c->d_minel);
+  IB3D_CUDA(c, cudaGetLastError());
+  c->retagged = nlist;
+  return finish_search(c, bi0, bj0, bk0, bni, bnj, bnk);
+}
+
+namespace {
+// The part of the search after the flags are set: counts, the lexicographic IB list
+// over the box (every IB cell lies in it), the normal distances and the ghost-point
+// schedules.
+int finish_search(ib3d_ctx* c, int bi0, int bj0, int bk0, int bni, int bnj, int bnk) {
+  const Dims& d = c->d;
+  const unsigned nbox = (unsigned)bni * bnj * bnk;
+  const int ne = (int)c->nelems;
+  IB3D_CUDA(c, cudaMemsetAsync(c->ibmap, 0xff, sizeof(int) * (size_t)d.n3, c->st));
   // counts
   unsigned long long* dcount = reinterpret_cast<unsigned long long*>(c->d_scan);
   IB3D_CUDA(c, cudaMemsetAsync(dcount, 0, 5 * sizeof(unsigned long long), c->st));
@@ -742,13 +908,8 @@ int run_search(ib3d_ctx* c) {
   IB3D_CUDA(c, cudaMalloc(&c->d_nelp, sizeof(int) * (size_t)std::max(nib, 1)));
   IB3D_CUDA(c, cudaMalloc(&c->d_nd, sizeof(double) * 7 * (size_t)std::max(nib, 1)));
   const unsigned nb = nblk(nbox);
+  if (int rc = ensure_scan(c, nb)) return rc;
   long long* boff = c->d_scan + 8;
-  if ((size_t)nb + 9 > c->scan_cap) {
-    cudaFree(c->d_scan);
-    c->scan_cap = (size_t)nb + 64;
-    IB3D_CUDA(c, cudaMalloc(&c->d_scan, sizeof(long long) * c->scan_cap));
-    boff = c->d_scan + 8;
-  }
   k_ib_blockcount<<<nb, kBlock, 0, c->st>>>(d, c->cell, bi0, bj0, bk0, bni, bnj, nbox, boff);
   k_exclusive_scan<<<1, 1024, 0, c->st>>>(boff, (int)nb, c->d_scan);
   k_ib_scatter<<<nb, kBlock, 0, c->st>>>(d, c->cell, bi0, bj0, bk0, bni, bnj, nbox, boff, nib, c->d_iblist);
@@ -784,6 +945,7 @@ int run_search(ib3d_ctx* c) {
   }
   return IB3D_OK;
 }
+}  // namespace
 
 int run_velocity_forcing(ib3d_ctx* c) {
   PhaseScope ps(c, PH_FORCING);

@@ -193,6 +193,17 @@ int ib3d_move_body_free(ib3d_ctx* ctx, double fx, double fy, double fz, double v
  * counts (may be NULL) = {fluid, solid, ib, red, black}. */
 int ib3d_search(ib3d_ctx* ctx, const int64_t box[6], int64_t counts[5]);
 
+/* selectiveRetagging (subSearch.f90:327-512), for a body that moves a little each step:
+ * the tagging test runs only on the 6x6x6 neighbourhood i-2..i+3, j-2..j+3, k-2..k+3
+ * of every cell of the current IB list (clipped to the interior); every other cell
+ * keeps its flag. Then cellCount, computeNormDistance and the ghost-point schedule as
+ * ib3d_search runs them. Call it after ib3d_move_body in place of ib3d_search; it
+ * needs the IB list of an earlier ib3d_search (or ib3d_selective_retag) of the same
+ * mesh. Its flags equal a full search's whenever every cell whose flag changes lies
+ * within those neighbourhoods (a body moving less than about two cells per call).
+ * counts (may be NULL) as ib3d_search. */
+int ib3d_selective_retag(ib3d_ctx* ctx, int64_t counts[5]);
+
 /* Parity read-back of the search: cell flags (nx+2,ny+2,nz+2) int64 as in `cell`
  * (modGlobal.f90:25), interceptedIndexPtr (nib,3), nelp (nib) and the seven normal
  * distances (7 x nib: p, u1, u2, v1, v2, w1, w2). Any pointer may be NULL. */

@@ -50,6 +50,60 @@ def test_oscillating_body_bit_exact(ib3d, oracle_mod, grids, name):
     s.close()
 
 
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_selective_retagging_bit_exact_and_equal_to_the_full_search(ib3d, oracle_mod, grids, name):
+    """selectiveRetagging (subSearch.f90:327-512) every step of the oscillating body:
+    the CUDA path re-tags only the 6^3 neighbourhoods of the IB cells and must match
+    the oracle's restatement of the same routine bit for bit (counts, flags, IB list,
+    nearest elements, normal distances, sweeps, drag/lift, fields), and a third
+    context re-tagging its whole box after the same moves must reach the same flags
+    and lists (the body moves less than a core cell per step)."""
+    cs = grids.case(name)
+    s, o = _pair(ib3d, oracle_mod, cs)
+    full = ib3d.setup_case(cs)
+    amp, freq = 0.15, 5.0
+    flags0 = s.get_search()["cell"]
+    changed = 0
+    for step in range(1, 9):
+        y0, _ = motion((step - 1) * cs.dt, amp, freq)
+        y1, v1 = motion(step * cs.dt, amp, freq)
+        for x in (s, o, full):
+            x.move_body(0.0, y1 - y0, 0.0, 0.0, v1, 0.0)
+        cg = s.selective_retag()
+        assert cg == o.selective_retag(), step
+        assert cg == full.search(grids.body_box(cs, (0.0, y1, 0.0))), step
+        gs, os_, gf = s.get_search(), o.get_search(), full.get_search()
+        for key in ("cell", "ib", "nelp", "normdis"):
+            _same(gs[key], os_[key], f"step {step} {key} vs oracle")
+            _same(gs[key], gf[key], f"step {step} {key} vs full search")
+        changed = max(changed, int(np.count_nonzero(gs["cell"] != flags0)))
+        gst, gcoef = s.step(step == 1)
+        ost, ocoef = o.step(step == 1)
+        assert gst["sweeps"] == ost["sweeps"], step
+        assert np.array_equal(gcoef, ocoef), (step, gcoef, ocoef)
+    for f in FIELDS:
+        _same(s.get_field(f), o.get_field(f), f"after 8 moving steps {f}")
+    assert changed > 0, "the motion never changed a flag"
+    for x in (s, full):
+        x.close()
+
+
+def test_selective_retag_needs_an_ib_list_of_the_same_mesh(ib3d, grids):
+    cs = grids.case("tiny")
+    s = ib3d.Solver(cs.x, cs.y, cs.z)
+    nodes, tris = grids.icosphere(cs.subdivisions, cs.radius)
+    s.set_mesh(nodes, tris)
+    with pytest.raises(ib3d.IB3DError):
+        s.selective_retag()
+    s.search(cs.box)
+    s.move_body(0.0, 0.01, 0.0)
+    s.selective_retag()
+    s.set_mesh(nodes, tris)
+    with pytest.raises(ib3d.IB3DError):
+        s.selective_retag()
+    s.close()
+
+
 def test_step_requires_search_after_move(ib3d, grids):
     cs = grids.case("tiny")
     s = ib3d.setup_case(cs)
