@@ -695,6 +695,9 @@ def main():
     ap.add_argument("--sweep-bench", action="store_true",
                     help="instead of the step benchmark: microseconds per FP32 sweep of each sweep kernel on the "
                          "256x192x192 and 384x256x256 workloads")
+    ap.add_argument("--sweep-cases", default="sphere256,sphere384", help="workloads of --sweep-bench")
+    ap.add_argument("--sweep-kernels", default="0,2", help="sweep kernels of --sweep-bench")
+    ap.add_argument("--sweep-steps", type=int, default=3, help="timed steps of --sweep-bench per workload and kernel")
     ap.add_argument("--poisson", type=int, default=0,
                     help="instead of the step benchmark: the standalone all-Neumann Poisson cube of this edge "
                          "(omega 1.85, residual 1e-8), FP64 and FP32-sweep forms")
@@ -768,7 +771,9 @@ def main():
         return
     if args.sweep_bench:
         if dist.rank == 0:
-            print(json.dumps(sweep_bench(pkg)), flush=True)
+            print(json.dumps(sweep_bench(pkg, tuple(args.sweep_cases.split(",")),
+                                         tuple(int(k) for k in args.sweep_kernels.split(",")), args.sweep_steps)),
+                  flush=True)
         dist.close()
         return
     if args.poisson:

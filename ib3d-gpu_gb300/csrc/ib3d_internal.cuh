@@ -71,6 +71,7 @@ struct SolveCtl {
   long long nsweeps;          // sweep at which the loop stopped
   double final_err;           // stopping-test value at that sweep
   double last_res;            // last residual measured
+  int stage_err;              // a staged sweep's bulk-copy wait gave up (the pass's results are invalid)
 };
 
 // Body motion seen by the forcing: the surface velocity (usurf, vsurf, wsurf of

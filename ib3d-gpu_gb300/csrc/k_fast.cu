@@ -368,7 +368,8 @@ int run_sor_fp64_fast(ib3d_ctx* c, ib3d_solve_stats* st) {
 
 void launch_residual_fast(ib3d_ctx* c, long long sweep) {
   const Dims& d = c->d;
-  const bool packed = c->prm.sweep_kernel == 0 && c->ep[0] != nullptr;
+  // the colour-packed sweeps (kernels 0 and 2) read the packed right-hand side
+  const bool packed = c->prm.sweep_kernel != 1 && c->ep[0] != nullptr;
   c->launches += 1;
   k_residual_fast<<<nblk((long long)d.nx * d.ny * d.nz), kBlock, 0, c->st>>>(
       d, c->g, c->bdt, c->pc, c->cell, packed ? nullptr : c->r32, packed ? c->rp[0] : nullptr,

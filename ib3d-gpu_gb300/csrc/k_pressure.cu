@@ -477,7 +477,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   const bool packed = (P.sweep_kernel == 0 || fused) && c->ep[0] != nullptr;
   if (fused) {
     if (!packed || !fused_sweep_fits(d.nx)) {
-      c->err = "sweep_kernel 2 (fused sweep) needs an even nx of at most 1280 cells";
+      c->err = "sweep_kernel 2 (fused sweep) needs an even nx whose packed rows fit its blocks (nx <= 512)";
       return IB3D_ERR_ARG;
     }
     if (!c->epn[0]) {
@@ -502,6 +502,10 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
     IB3D_CUDA(c, cudaGetLastError());
     rc = read_ctl(c);
     if (rc) return rc;
+    if (c->h_ctl->stage_err) {
+      c->err = "fused FP32 sweep: a shared-memory stage never arrived (bounded wait gave up)";
+      return IB3D_ERR_CUDA;
+    }
     const double res = c->h_ctl->last_res;
     if (outer == 0) st->initial_err = res;
     if (c->h_ctl->done) break;

@@ -140,25 +140,38 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
 }
 
 // One whole red-black sweep per launch: the red pass and the black pass fused into a
-// z-wavefront. A block owns kFY rows (j) by kFZ planes (k) over the full x extent of
-// the packed rows (blockDim.x = 32 x warps, one float4 group per thread; blockDim.y
-// = kFY + 2 rows) and marches k upward. At plane k every row thread updates the red
-// cells of its row from the black values before the sweep (planes k-1, k, k+1 kept in
-// registers, the rows j+-1 loaded), puts the new red row into a three-plane ring in
-// shared memory, and after one barrier the inner rows update their black cells of
-// plane k-1 from the new red values (rows j+-1 from the ring, planes k-2 and k from
-// registers). Black at the block's edges needs new red values one row and one plane
-// beyond the block, so those are computed by this block too (the neighbouring blocks
-// compute the same values). Every block therefore reads the values before the sweep
-// from one pair of arrays (e_red, e_black) and writes the new values to a second pair
-// (n_red, n_black): no block overwrites what another still has to read, and the
-// caller swaps the pairs after each sweep. Every fluid cell is written by exactly one
-// block; the other entries hold 0 in both pairs. Per cell the arithmetic is
-// update4's, in the same order, so the results are bit-identical to two k_sor32p
-// passes. Each array is read once per sweep (plus the halo rows and planes), against
-// the other colour's array twice in the two-pass form.
-constexpr int kFY = 8;
+// z-wavefront over planes staged in shared memory.
+//
+// A block owns FY rows (j) by kFZ planes (k) over the full x extent of the packed
+// rows (blockDim.x = 32 x warps, one float4 group per thread; blockDim.y = FY + 2
+// row threads, the outer two for halo rows) and marches k upward. For every plane p
+// one thread copies the block's rows of the four arrays into a shared-memory stage
+// with 1-D bulk asynchronous copies (cp.async.bulk, completion counted on the
+// stage's mbarrier): black before the sweep on rows j0-2..j0+FY+1, red before the
+// sweep and the red right-hand side on rows j0-1..j0+FY, the black right-hand side
+// on rows j0..j0+FY-1. S stages rotate, so the copies of planes up to k+S-2 are in
+// flight while plane k is computed, and the threads read only shared memory: the
+// load path serves hits, with no cache misses to fill.
+//
+// At plane k every row thread updates the red cells of its row from the black values
+// before the sweep (planes k-1 and k carried in registers, k+1 and the rows j+-1
+// read from the stages) and puts the new red row into a three-plane ring; after one
+// barrier the inner rows update their black cells of plane k-1 from the new red
+// values (rows j+-1 from the ring, planes k-2 and k from registers). Black at the
+// block's edges needs new red values one row and one plane beyond the block, so those
+// are computed by this block too (the neighbouring blocks compute the same values).
+// Every block therefore reads the values before the sweep from one pair of arrays
+// (e_red, e_black) and writes the new values to a second pair (n_red, n_black): no
+// block overwrites what another still has to read, and the caller swaps the pairs
+// after each sweep. Every fluid cell is written by exactly one block; the other
+// entries hold 0 in both pairs. Per cell the arithmetic is update4's, in the same
+// order, so the results are bit-identical to two k_sor32p passes.
+//
+// Every mbarrier wait is bounded and decided for the whole block: a wait that gives
+// up sets ctl->stage_err (the host fails the solve), stops the issue of copies, and
+// the block waits (bounded) for the copies it has issued before it exits.
 constexpr int kFZ = 16;
+constexpr int kMaxStages = 6;
 
 template <bool FIRST>
 __device__ __forceinline__ void update_group(const float4 r4, float4& e4, const float (&ox)[6], const float4 s4,
@@ -175,110 +188,221 @@ __device__ __forceinline__ void update_group(const float4 r4, float4& e4, const 
   e4 = make_float4(ev[0], ev[1], ev[2], ev[3]);
 }
 
-__global__ void __launch_bounds__(640) k_sor32f(Dims d, Grid1D g, const float* __restrict__ r_red,
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Bounded wait on an mbarrier phase (true when it completed).
+__device__ __forceinline__ bool stage_wait(unsigned long long* bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned ok;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+template <int FY, int S>
+__global__ void __launch_bounds__(640) k_sor32t(Dims d, Grid1D g, const float* __restrict__ r_red,
                                                  const float* __restrict__ r_black,
                                                  const float* __restrict__ e_red, const float* __restrict__ e_black,
                                                  float* __restrict__ n_red, float* __restrict__ n_black, int Lp,
-                                                 float omega, float om1) {
-  extern __shared__ float4 ring[];   // [3][kFY + 2][blockDim.x]
+                                                 float omega, float om1, SolveCtl* ctl) {
+  static_assert(S >= 4 && S <= kMaxStages, "a stage is refilled two planes after it is last read");
+  extern __shared__ __align__(128) float smf[];   // [S][(4 FY + 8) Lp] stages, then the ring
+  __shared__ __align__(8) unsigned long long bar[kMaxStages];
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nq = ((d.nx >> 1) + 3) >> 2;
   const int nqp = blockDim.x;
   const int q = threadIdx.x, lane = q & 31;
-  const int tr = threadIdx.y;                       // 0 and kFY + 1: halo rows
-  const int j = blockIdx.x * kFY + 1 + tr;          // row of this thread
+  const int tr = threadIdx.y;                       // 0 and FY + 1: halo rows
+  const bool lead = q == 0 && tr == 0;
+  const int j0 = blockIdx.x * FY + 2;               // first row the block owns
+  const int j = j0 - 1 + tr;                        // row of this thread
   const int k0 = blockIdx.y * kFZ + 2;              // first plane the block owns
   const int k1 = min(k0 + kFZ, d.nz + 2);           // one past the last
+  const int kr0 = k0 - 1;                           // first red plane (a halo plane, or the ghost plane)
   const bool row_cell = j >= 2 && j <= d.ny + 1;    // the row holds cells (not a ghost row)
-  const bool row_in = j <= d.ny + 2;                // the row exists in the arrays
-  const bool inner = tr >= 1 && tr <= kFY && row_cell;
-  const bool active = q < nq && row_in;
+  const bool inner = tr >= 1 && tr <= FY && row_cell;
+  const bool active = q < nq && j <= d.ny + 2;
   const bool load_left = lane == 0, load_right = lane == 31 || q + 1 >= nq;
   const int plane = (d.ny + 2) * Lp;
-  const int sj = (j - 1) * Lp + 4 * q + 4;
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int e = 4 * q + 4;                          // this thread's first entry within a row
+  const int stage_floats = (4 * FY + 8) * Lp;
+  float4* ring = reinterpret_cast<float4*>(smf + S * stage_floats);   // [3][FY + 2][nqp]
+  // rows copied into a stage (clipped to the arrays' rows 1..ny+2; rows outside are never read)
+  const int eb_lo = max(1, j0 - 2), eb_hi = min(d.ny + 2, j0 + FY + 1);
+  const int er_lo = max(1, j0 - 1), er_hi = min(d.ny + 2, j0 + FY);
+  const int rb_lo = j0, rb_hi = min(d.ny + 1, j0 + FY - 1);
+  // this thread's entries within a stage: black row j, red and r_red row j, r_black row j
+  const int o_eb = (tr + 1) * Lp + e, o_er = (FY + 4 + tr) * Lp + e, o_rr = (2 * FY + 6 + tr) * Lp + e,
+            o_rb = (3 * FY + 8 + tr - 1) * Lp + e;
+  const unsigned stage_bytes =
+      (unsigned)((eb_hi - eb_lo + 1) + 2 * (er_hi - er_lo + 1) + (rb_hi - rb_lo + 1)) * (unsigned)Lp * 4u;
+  const int pbase = kr0 - 1, plast = k1 + 1;        // planes the block reads
+  if (lead) {
+    for (int s = 0; s < S; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar[s])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // Planes pbase..plast pass through the stages in order (plane p in stage (p - pbase)
+  // mod S), each once through its stage's mbarrier, so that the n-th use of a stage is
+  // the barrier's phase n: a plane outside the arrays (the ghost-side halo planes 0 and
+  // nz+3) only arrives, and its stage is never read.
+  int istage = 0;   // stage of the next plane to issue (lead thread)
+  auto issue = [&](int p) {
+    float* st = smf + istage * stage_floats;
+    unsigned long long* b = &bar[istage];
+    istage = istage + 1 == S ? 0 : istage + 1;
+    if (p < 1 || p > d.nz + 2) {
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(b)) : "memory");
+      return;
+    }
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(b)), "r"(stage_bytes)
+                 : "memory");
+    const long long pl = (long long)(p - 1) * plane;
+    bulk_copy(st + (eb_lo - (j0 - 2)) * Lp, e_black + pl + (long long)(eb_lo - 1) * Lp,
+              (unsigned)(eb_hi - eb_lo + 1) * Lp * 4u, b);
+    bulk_copy(st + (FY + 4 + er_lo - (j0 - 1)) * Lp, e_red + pl + (long long)(er_lo - 1) * Lp,
+              (unsigned)(er_hi - er_lo + 1) * Lp * 4u, b);
+    bulk_copy(st + (2 * FY + 6 + er_lo - (j0 - 1)) * Lp, r_red + pl + (long long)(er_lo - 1) * Lp,
+              (unsigned)(er_hi - er_lo + 1) * Lp * 4u, b);
+    bulk_copy(st + (3 * FY + 8 + rb_lo - j0) * Lp, r_black + pl + (long long)(rb_lo - 1) * Lp,
+              (unsigned)(rb_hi - rb_lo + 1) * Lp * 4u, b);
+  };
+  // block-uniform wait for the next plane in order; false when it gave up
+  int wstage = 0;
+  unsigned wparity = 0;   // bit s: parity of the next phase of stage s
+  auto wait_next = [&]() {
+    const bool ok = stage_wait(&bar[wstage], (wparity >> wstage) & 1u);
+    wparity ^= 1u << wstage;
+    wstage = wstage + 1 == S ? 0 : wstage + 1;
+    return __syncthreads_and(ok) != 0;
+  };
+  int issued = pbase - 1, waited = pbase - 1;       // last plane issued / waited for (block-uniform)
+  for (int p = pbase; p < pbase + S && p <= plast; ++p) {
+    if (lead) issue(p);
+    issued = p;
+  }
+  // x coefficients of this thread's four cells in both row phases
+  float4 axc[2][3];
+#pragma unroll
+  for (int sp = 0; sp < 2; ++sp)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) axc[sp][c] = q < nq ? g.axp[sp][c][q] : make_float4(0.f, 0.f, 0.f, 0.f);
   float ay0 = 0.f, ay1 = 0.f, ay2 = 0.f;
   if (row_cell) {
     ay0 = g.acy32[0][j - 1];
     ay1 = g.acy32[1][j - 1];
     ay2 = g.acy32[2][j - 1];
   }
-  float4* ringp = ring + tr * nqp + q;
-  const int ring_plane = (kFY + 2) * nqp;
-  // black values before the sweep at planes k-1 and k of this row (registers), for
-  // the first red plane k0-1 (the ghost plane when k0 = 2: no red update there)
-  const int kr0 = k0 - 1;
-  float4 bm = z4, b0 = z4;
-  if (active && kr0 >= 2) {
-    bm = *reinterpret_cast<const float4*>(e_black + (kr0 - 2) * plane + sj);
-    b0 = *reinterpret_cast<const float4*>(e_black + (kr0 - 1) * plane + sj);
-  } else if (active) {
-    b0 = *reinterpret_cast<const float4*>(e_black + (kr0 - 1) * plane + sj);
+  bool ok = true;
+  // planes kr0-1 and kr0 before the first red plane
+  for (int p = pbase; p <= kr0 && ok; ++p) {
+    ok = wait_next();
+    waited = p;
   }
-  float4 rm2 = z4, rm1 = z4;   // new red values at planes k-2, k-1 of this row
-  for (int k = kr0; k <= k1; ++k) {
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 bm = z4, b0 = z4, rm2 = z4, rm1 = z4;
+  if (ok && row_cell && active) {
+    if (kr0 - 1 >= 1) bm = *reinterpret_cast<const float4*>(smf + o_eb);                 // stage 0
+    if (kr0 >= 1) b0 = *reinterpret_cast<const float4*>(smf + stage_floats + o_eb);     // stage 1
+  }
+  // stages of planes k-1, k, k+1 and ring slots of planes k-1, k, rotated each plane
+  int s_m = 0, s_0 = 1, s_p = 2 % S;
+  int ring_m = 2, ring_0 = 0;
+  float4* ringp = ring + tr * nqp + q;
+  const int ring_plane = (FY + 2) * nqp;
+  for (int k = kr0; k <= k1 && ok; ++k) {
+    ok = wait_next();   // plane k+1
+    if (!ok) break;
+    waited = k + 1;
+    const float* st_p = smf + s_p * stage_floats;
+    const float* st_0 = smf + s_0 * stage_floats;
     // ---- red cells of plane k
     const bool plane_cell = k >= 2 && k <= d.nz + 1;
-    const int s0 = (k - 1) * plane + sj;
+    const int s0 = (k - 1) * plane + (j - 1) * Lp + e;
     float4 bp = z4;   // black before the sweep at plane k+1
-    if (active && k + 1 <= d.nz + 2) bp = *reinterpret_cast<const float4*>(e_black + s0 + plane);
+    if (row_cell && active && k + 1 <= d.nz + 2) bp = *reinterpret_cast<const float4*>(st_p + o_eb);
     float4 rn = z4;
-    const bool red_here = plane_cell && row_cell;   // warp-uniform
-    if (red_here) {
+    if (plane_cell && row_cell) {   // warp-uniform
       float left = __shfl_up_sync(0xffffffffu, b0.w, 1);
       float right = __shfl_down_sync(0xffffffffu, b0.x, 1);
       if (active) {
-        if (load_left) left = e_black[s0 - 1];
-        if (load_right) right = e_black[s0 + 4];
-        const float4 rr = *reinterpret_cast<const float4*>(r_red + s0);
-        rn = *reinterpret_cast<const float4*>(e_red + s0);
-        const float4 os = *reinterpret_cast<const float4*>(e_black + s0 - Lp);
-        const float4 on = *reinterpret_cast<const float4*>(e_black + s0 + Lp);
+        const float* rowb = st_0 + o_eb;
+        if (load_left) left = rowb[-1];
+        if (load_right) right = rowb[4];
+        const float4 rr = *reinterpret_cast<const float4*>(st_0 + o_rr);
+        rn = *reinterpret_cast<const float4*>(st_0 + o_er);
+        const float4 os = *reinterpret_cast<const float4*>(rowb - Lp);
+        const float4 on = *reinterpret_cast<const float4*>(rowb + Lp);
         const float oxa[6] = {left, b0.x, b0.y, b0.z, b0.w, right};
         const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
-        const bool own_first = ((j + k) & 1) == 1;   // red is (i+j+k) odd: does the row start with red?
-        const int sp = own_first ? 0 : 1;
-        const float4 a0 = g.axp[sp][0][q], a1 = g.axp[sp][1][q], a2 = g.axp[sp][2][q];
-        if (own_first)
-          update_group<true>(rr, rn, oxa, os, on, bm, bp, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
+        if (((j + k) & 1) == 1)   // red is (i+j+k) odd: the row starts with red
+          update_group<true>(rr, rn, oxa, os, on, bm, bp, axc[0][0], axc[0][1], axc[0][2], ay0, ay1, ay2, az0, az1,
+                             az2, omega, om1);
         else
-          update_group<false>(rr, rn, oxa, os, on, bm, bp, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
+          update_group<false>(rr, rn, oxa, os, on, bm, bp, axc[1][0], axc[1][1], axc[1][2], ay0, ay1, ay2, az0,
+                              az1, az2, omega, om1);
         if (inner && k >= k0 && k < k1) *reinterpret_cast<float4*>(n_red + s0) = rn;
       }
     }
-    const int slot = (k - kr0) % 3;
-    ringp[slot * ring_plane] = rn;
+    ringp[ring_0 * ring_plane] = rn;
     __syncthreads();
+    // every thread is past plane k-1's red update and plane k-2's black update: the
+    // stage of plane k-2 is free for plane k-2+S
+    if (k >= kr0 + 1) {
+      const int pn = k - 2 + S;
+      if (pn <= plast) {
+        if (lead) issue(pn);
+        issued = pn;
+      }
+    }
     // ---- black cells of plane k-1, from the new red values
     const int kb = k - 1;
     if (inner && kb >= k0 && kb < k1) {   // warp-uniform
-      const int slot_b = (kb - kr0) % 3;
-      const float4* rb_row = ring + slot_b * ring_plane + tr * nqp;
+      const float4* rb_row = ring + ring_m * ring_plane + tr * nqp;
       float left = __shfl_up_sync(0xffffffffu, rm1.w, 1);
       float right = __shfl_down_sync(0xffffffffu, rm1.x, 1);
       if (active) {
         if (load_left) left = q > 0 ? rb_row[q - 1].w : 0.f;
         if (load_right) right = q + 1 < nqp ? rb_row[q + 1].x : 0.f;
-        const int sb = s0 - plane;
-        const float4 rr = *reinterpret_cast<const float4*>(r_black + sb);
+        const float4 rr = *reinterpret_cast<const float4*>(smf + s_m * stage_floats + o_rb);
         float4 en = bm;   // black before the sweep at plane k-1
         const float4 os = rb_row[q - nqp], on = rb_row[q + nqp];
         const float oxa[6] = {left, rm1.x, rm1.y, rm1.z, rm1.w, right};
         const float az0 = g.acz32[0][kb - 1], az1 = g.acz32[1][kb - 1], az2 = g.acz32[2][kb - 1];
-        const bool own_first = ((j + kb) & 1) == 0;   // black is (i+j+k) even
-        const int sp = own_first ? 0 : 1;
-        const float4 a0 = g.axp[sp][0][q], a1 = g.axp[sp][1][q], a2 = g.axp[sp][2][q];
-        if (own_first)
-          update_group<true>(rr, en, oxa, os, on, rm2, rn, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
+        if (((j + kb) & 1) == 0)   // black is (i+j+k) even: the row starts with black
+          update_group<true>(rr, en, oxa, os, on, rm2, rn, axc[0][0], axc[0][1], axc[0][2], ay0, ay1, ay2, az0, az1,
+                             az2, omega, om1);
         else
-          update_group<false>(rr, en, oxa, os, on, rm2, rn, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
-        *reinterpret_cast<float4*>(n_black + sb) = en;
+          update_group<false>(rr, en, oxa, os, on, rm2, rn, axc[1][0], axc[1][1], axc[1][2], ay0, ay1, ay2, az0,
+                              az1, az2, omega, om1);
+        *reinterpret_cast<float4*>(n_black + s0 - plane) = en;
       }
     }
     bm = b0;
     b0 = bp;
     rm2 = rm1;
     rm1 = rn;
+    s_m = s_0;
+    s_0 = s_p;
+    s_p = s_p + 1 == S ? 0 : s_p + 1;
+    ring_m = ring_0;
+    ring_0 = ring_0 == 2 ? 0 : ring_0 + 1;
+  }
+  if (!ok) {
+    if (lead) atomicExch(&ctl->stage_err, 1);
+    // let the copies still in flight land before the block's shared memory is released
+    for (int p = waited + 1; p <= issued; ++p) {
+      stage_wait(&bar[wstage], (wparity >> wstage) & 1u);
+      wparity ^= 1u << wstage;
+      wstage = wstage + 1 == S ? 0 : wstage + 1;
+    }
   }
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
@@ -329,32 +453,81 @@ void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
     cudaLaunchKernelEx(&cfg, k_sor32p<1>, d, c->g, r, e, o, c->packed_lp, omega, om1);
 }
 
+// Rows per block and stages of the staged sweep for a row of nq float4 groups: 16 rows
+// with up to five stages where the shared memory holds them, else 8 rows.
+struct StagedShape {
+  int fy, stages, wx;
+  size_t smem;
+};
+static size_t staged_smem(int fy, int S, int Lp, int wx) {
+  return (size_t)S * (4 * fy + 8) * Lp * sizeof(float) + (size_t)3 * (fy + 2) * 32 * wx * sizeof(float4);
+}
+static bool staged_shape(int nx, StagedShape& out) {
+  const int nq = ((nx >> 1) + 3) >> 2, wx = (nq + 31) / 32, Lp = packed_row_length(nx);
+  const size_t cap = 227 * 1024 - 256;   // shared memory per block, less the static barriers
+  // one block per SM with the deepest staging that fits: tried at 256x192x192, two
+  // blocks of 8 rows and 4 stages per SM ran 35.6 us per sweep against 28.5 us for one
+  // block of 16 rows and 5 stages
+  for (size_t share : {cap})
+    for (int fy : {16, 8}) {
+      if (32 * wx * (fy + 2) > 640) continue;
+      for (int S = 5; S >= 4; --S)
+        if (staged_smem(fy, S, Lp, wx) <= share) {
+          out = {fy, S, wx, staged_smem(fy, S, Lp, wx)};
+          return true;
+        }
+    }
+  return false;
+}
+
+// Largest nx the fused sweep takes: its block spans a whole packed row, and four
+// stages of it fit in shared memory.
+bool fused_sweep_fits(int nx) {
+  StagedShape sh;
+  return staged_shape(nx, sh);
+}
+
 // One fused sweep: reads the sweep's input from ep[], writes its result to epn[] and
 // swaps the two pairs, so ep[] holds the current correction afterwards.
 void launch_sor32_fused(ib3d_ctx* c, float omega, float om1) {
   const Dims& d = c->d;
-  const int nq = ((d.nx >> 1) + 3) >> 2;
-  const int wx = (nq + 31) / 32;
-  const dim3 grid((unsigned)((d.ny + kFY - 1) / kFY), (unsigned)((d.nz + kFZ - 1) / kFZ)),
-      block((unsigned)(32 * wx), (unsigned)(kFY + 2));
+  StagedShape sh;
+  if (!staged_shape(d.nx, sh)) return;   // checked before the solve starts
+  const dim3 grid((unsigned)((d.ny + sh.fy - 1) / sh.fy), (unsigned)((d.nz + kFZ - 1) / kFZ)),
+      block((unsigned)(32 * sh.wx), (unsigned)(sh.fy + 2));
+  static bool smem_set = false;   // more than the default 48 KB of dynamic shared memory
+  if (!smem_set) {
+    const int mx = 227 * 1024 - 256;
+    cudaFuncSetAttribute(k_sor32t<16, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_sor32t<16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_sor32t<8, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_sor32t<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    smem_set = true;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
-  cfg.dynamicSmemBytes = sizeof(float4) * 3 * (kFY + 2) * 32 * wx;
+  cfg.dynamicSmemBytes = sh.smem;
   cfg.stream = c->st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_sor32f, d, c->g, (const float*)c->rp[0], (const float*)c->rp[1],
-                     (const float*)c->ep[0], (const float*)c->ep[1], c->epn[0], c->epn[1], c->packed_lp, omega, om1);
+  const float *rr = c->rp[0], *rb = c->rp[1], *er = c->ep[0], *eb = c->ep[1];
+  float *nr = c->epn[0], *nb = c->epn[1];
+  const int Lp = c->packed_lp;
+  if (sh.fy == 16 && sh.stages == 5)
+    cudaLaunchKernelEx(&cfg, k_sor32t<16, 5>, d, c->g, rr, rb, er, eb, nr, nb, Lp, omega, om1, c->ctl);
+  else if (sh.fy == 16)
+    cudaLaunchKernelEx(&cfg, k_sor32t<16, 4>, d, c->g, rr, rb, er, eb, nr, nb, Lp, omega, om1, c->ctl);
+  else if (sh.stages == 5)
+    cudaLaunchKernelEx(&cfg, k_sor32t<8, 5>, d, c->g, rr, rb, er, eb, nr, nb, Lp, omega, om1, c->ctl);
+  else
+    cudaLaunchKernelEx(&cfg, k_sor32t<8, 4>, d, c->g, rr, rb, er, eb, nr, nb, Lp, omega, om1, c->ctl);
   std::swap(c->ep[0], c->epn[0]);
   std::swap(c->ep[1], c->epn[1]);
 }
-
-// Largest nx the fused sweep takes: its block spans a whole packed row.
-bool fused_sweep_fits(int nx) { return ((((nx >> 1) + 3) >> 2) + 31) / 32 * 32 * (kFY + 2) <= 640; }
 
 void launch_accumulate_packed(ib3d_ctx* c) {
   const long long n = (long long)c->d.nx * c->d.ny * c->d.nz;

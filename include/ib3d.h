@@ -83,7 +83,7 @@ typedef struct ib3d_params {
   int32_t inner_sweeps; /* FP32 sweeps per defect-correction pass (IB3D_PREC_FP32DC) */
   int32_t sweep_kernel; /* FP32 sweep kernel: 0 colour-packed arrays, one launch per colour pass (even
                            nx); 1 the padded field layout; 2 colour-packed arrays, the red and black
-                           passes fused into one z-wavefront launch per sweep (even nx <= 1280) */
+                           passes fused into one z-wavefront launch per sweep (even nx <= 512) */
   double omega_inner;   /* relaxation factor of the FP32 inner sweeps (0: use omega). The FP64
                            defect correction fixes the final accuracy, so the inner solve may use
                            its own factor. */
