@@ -544,6 +544,63 @@ def sweep_bench(pkg, cases=("sphere256", "sphere384"), kernels=(0, 2), steps: in
     return out
 
 
+# the U-Net's convolutions (input channels K, output channels N, level 1-3) in layer order
+UNET_CONVS = [(16, 16, 1), (16, 16, 1), (16, 32, 2), (32, 32, 2), (32, 64, 3), (64, 64, 3), (96, 32, 2),
+              (32, 32, 2), (48, 16, 1), (16, 16, 1)]
+
+
+def unet_train_flops(batch: int, s: int) -> float:
+    """FLOPs of one Adam step's convolutions as the kernels compute them (the first
+    layer's 4 input channels padded to 16): forward 2*27*K*N per voxel of its level,
+    the weight gradient the same, the input gradient the same for every layer but the
+    first."""
+    total = 0.0
+    for q, (k, n, lvl) in enumerate(UNET_CONVS):
+        vox = batch * (s >> (lvl - 1)) ** 3
+        f = 2.0 * 27 * k * n * vox
+        total += f * (2 if q == 0 else 3)
+    return total
+
+
+def train_bench(pkg, seconds: float = 15.0, batch: int = 8) -> dict:
+    """Adam steps of the warm-start U-Net on patches captured from the 256x192x192
+    sphere (4x4x4 coarsening, 32^3-voxel patches of 128^3 cells), timed with the weight
+    gradients on the tensor cores and on the CUDA cores: steps/s and TFLOP/s of the
+    convolutions against the measured BF16 peak."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    cs = workload(pkg, "sphere256")
+    net = pkg.Net(seed=0)
+    net.set_coarsening(4)
+    S = 32
+    net.reserve(S, 96)
+    s = pkg.setup_case(cs, **FAST)
+    s.enable_history()
+    for n in range(8):
+        s.step(n == 0)
+        if n >= 2:
+            net.capture(s, 16, seed=n)
+    s.close()
+    flops = unet_train_flops(batch, S)
+    out = {"workload": f"U-Net training: batch {batch} patches of {S}^3 voxels (4x4x4 coarsening of 128^3 cells), "
+                       f"{net.dataset_size()} patches captured from the sphere256 run",
+           "gflop_per_step": flops / 1e9, "peak_tflops": peak,
+           "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if "bf16_tflops" in peaks else "fallback"}
+    for name, tc in (("tensor_core_wgrad", True), ("cuda_core_wgrad", False)):
+        net.set_wgrad_tensor_cores(tc)
+        net.train(5, batch=batch, lr=1e-4, seed=1)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            net.train(20, batch=batch, lr=1e-4, seed=100 + n)
+            n += 20
+        dt = time.perf_counter() - t0
+        out[name] = {"adam_steps_per_s": n / dt, "tflops": n * flops / dt / 1e12,
+                     "frac_of_peak": n * flops / dt / 1e12 / peak}
+    net.set_wgrad_tensor_cores(True)
+    net.close()
+    return out
+
+
 def compare_fp64(pkg, cs, steps: int, net=None) -> dict:
     """The mixed-precision form (the bench's FP32 arm, learned warm start when a
     network is given) against the plain FP64 path over the same `steps` steps, both to
@@ -695,6 +752,8 @@ def main():
     ap.add_argument("--sweep-bench", action="store_true",
                     help="instead of the step benchmark: microseconds per FP32 sweep of each sweep kernel on the "
                          "256x192x192 and 384x256x256 workloads")
+    ap.add_argument("--train-bench", action="store_true",
+                    help="instead of the step benchmark: Adam steps/s and TFLOP/s of the warm-start network's training")
     ap.add_argument("--sweep-cases", default="sphere256,sphere384", help="workloads of --sweep-bench")
     ap.add_argument("--sweep-kernels", default="0,2", help="sweep kernels of --sweep-bench")
     ap.add_argument("--sweep-steps", type=int, default=3, help="timed steps of --sweep-bench per workload and kernel")
@@ -767,6 +826,12 @@ def main():
             if mnet is not None:
                 out["speedup_learned_vs_plain_fast"] = out["fp32_learned"]["value"] / out["plain_fp64_fast"]["value"]
             print(json.dumps(out), flush=True)
+        dist.close()
+        return
+    if args.train_bench:
+        if dist.rank == 0:
+            print(json.dumps(train_bench(pkg, args.train_seconds if args.train_seconds != 300.0 else 15.0)),
+                  flush=True)
         dist.close()
         return
     if args.sweep_bench:

@@ -152,6 +152,7 @@ def lib() -> C.CDLL:
         "ib3d_net_capture": (C.c_int, [_VP, _VP, C.c_int, C.c_uint64]),
         "ib3d_net_set_coarsening": (C.c_int, [_VP, C.c_int]),
         "ib3d_net_train": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_uint64, _D]),
+        "ib3d_net_set_wgrad_tensor_cores": (C.c_int, [_VP, C.c_int]),
         "ib3d_enable_history": (C.c_int, [_VP]),
         "ib3d_attach_net": (C.c_int, [_VP, _VP]),
         "ib3d_pressure_solve_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, _VP, _VP, _VP, _VP, _VP,
@@ -474,6 +475,11 @@ class Net:
 
     def capture(self, solver: "Solver", npatches: int, seed: int = 0):
         self._check(self.L.ib3d_net_capture(self._h, solver._h, npatches, seed), "ib3d_net_capture")
+
+    def set_wgrad_tensor_cores(self, on: bool = True):
+        """Weight gradients on the tensor cores (default) or on the CUDA cores (reference)."""
+        self._check(self.L.ib3d_net_set_wgrad_tensor_cores(self._h, 1 if on else 0),
+                    "ib3d_net_set_wgrad_tensor_cores")
 
     def train(self, steps: int, batch: int = 8, lr: float = 1e-3, seed: int = 0) -> float:
         loss = np.zeros(1)

@@ -16,8 +16,10 @@
 // MMAs, and a tcgen05.commit to the stage's mbarrier frees it for the stage after
 // next; the next stage's loads are in flight meanwhile. The
 // same kernel computes the input gradient with mirrored taps and transposed
-// weights. Weight gradients are reduced on the CUDA cores in FP32.
+// weights, and k_wgrad_tc the weight gradients as a second implicit GEMM over voxels.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "ib3d_internal.cuh"
 #include "unet.cuh"
@@ -233,7 +235,203 @@ __global__ void __launch_bounds__(128) k_conv3(Vol vol, Act X, int K, const bf16
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kCols));
 }
 
-// dW[n][tap][k] += sum_v dZ[v][n] * X[v + off(tap)][k]   (FP32, CUDA cores)
+// 8x8 transpose of BF16 values across the eight lanes of an octet (lanes 8m..8m+7):
+// on entry lane l holds row l (eight values, the first in the low half of v.x); on
+// return it holds column l. Three exchange rounds (lane distance 4, 2, 1), each
+// swapping the off-diagonal blocks of the next-smaller block size.
+__device__ __forceinline__ uint4 transpose8(uint4 v, int l8) {
+  unsigned w0 = v.x, w1 = v.y, w2 = v.z, w3 = v.w;
+  {
+    const bool up = l8 & 4;
+    const unsigned r0 = __shfl_xor_sync(0xffffffffu, up ? w0 : w2, 4);
+    const unsigned r1 = __shfl_xor_sync(0xffffffffu, up ? w1 : w3, 4);
+    if (up) { w0 = r0; w1 = r1; } else { w2 = r0; w3 = r1; }
+  }
+  {
+    const bool up = l8 & 2;
+    const unsigned r0 = __shfl_xor_sync(0xffffffffu, up ? w0 : w1, 2);
+    const unsigned r1 = __shfl_xor_sync(0xffffffffu, up ? w2 : w3, 2);
+    if (up) { w0 = r0; w2 = r1; } else { w1 = r0; w3 = r1; }
+  }
+  {
+    const bool up = l8 & 1;
+    const unsigned s0 = up ? __byte_perm(w0, w1, 0x5410) : __byte_perm(w0, w1, 0x7632);
+    const unsigned s1 = up ? __byte_perm(w2, w3, 0x5410) : __byte_perm(w2, w3, 0x7632);
+    const unsigned r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+    const unsigned r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+    if (up) {
+      w0 = __byte_perm(r0, w0, 0x7610); w1 = __byte_perm(r0, w1, 0x7632);
+      w2 = __byte_perm(r1, w2, 0x7610); w3 = __byte_perm(r1, w3, 0x7632);
+    } else {
+      w0 = __byte_perm(w0, r0, 0x5410); w1 = __byte_perm(w1, r0, 0x7610);
+      w2 = __byte_perm(w2, r1, 0x5410); w3 = __byte_perm(w3, r1, 0x7610);
+    }
+  }
+  return make_uint4(w0, w1, w2, w3);
+}
+
+// dW[n][tap][k] += sum_v dZ[v][n] * X[v + off(tap)][k] on the tensor cores: an
+// implicit GEMM D[r][n] = sum_v A[r][v] B[n][v] with the 27 K (tap, channel) pairs as
+// rows (128 per block, grid.x), the N output channels as columns and the voxels as the
+// reduction (a chunk of them per block, grid.y). A[r][v] = X[v + off(tap)][k] and
+// B[n][v] = dZ[v][n]; both tensors are channels-last, so an octet of threads loads
+// eight channels of eight consecutive voxels and transposes them (transpose8) into the
+// K-major core matrices the MMA reads. The pipeline is k_conv3's: kSub steps of 16
+// voxels per stage, two stages, one thread issuing tcgen05.mma kind::f16 into an FP32
+// accumulator in tensor memory, bounded mbarrier waits decided for the whole block. The
+// block adds its 128 x N partial sums to dW with FP32 atomics.
+template <int N>
+constexpr size_t wgrad_smem_bytes() {
+  return (size_t)2 * kSub * (128 * 16 + N * 16) * sizeof(bf16);
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_wgrad_tc(Vol vol, Act dZ, Act X, int K, float* __restrict__ dW,
+                                                  long long chunk, int* err) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 64, "output channels");
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  bf16* sA = reinterpret_cast<bf16*>(smraw);             // [2][kSub][128 * 16]
+  bf16* sB = sA + 2 * kSub * 128 * 16;                     // [2][kSub][N * 16]
+  __shared__ __align__(8) unsigned long long bar[3];
+  __shared__ unsigned tmem_base;
+  constexpr unsigned kCols = N <= 32 ? 32 : 64;
+  const int t = threadIdx.x, warp = t >> 5, oct = t >> 3, l8 = t & 7;
+  const long long M = vol.voxels();
+  const long long v0 = (long long)blockIdx.y * chunk, v1 = min(M, v0 + chunk);
+  const int rows = 27 * K;
+  const int R0 = blockIdx.x * 128 + 8 * oct;      // first (tap, channel) row of this octet
+  const bool rok = R0 < rows;
+  const int tap = rok ? R0 / K : 0, k0 = rok ? R0 % K : 0;   // K % 16 == 0: an octet's rows share the tap
+  const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  const bool bok = oct < N / 8;                   // this octet also stages eight rows of B
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_addr(&tmem_base)), "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (t == 0) {
+    for (int q = 0; q < 3; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&bar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = tmem_base;
+  // instruction descriptor: D FP32, A and B BF16, both K-major, N, M = 128
+  const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((128u >> 4) << 24);
+  const int steps = (int)((v1 - v0 + 15) / 16), nst = (steps + kSub - 1) / kSub;
+  uint4 ra[kSub][2], rb[kSub][2];
+  auto gather = [&](int q) {
+#pragma unroll
+    for (int j = 0; j < kSub; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        ra[j][h] = rb[j][h] = make_uint4(0, 0, 0, 0);
+        const int s = q * kSub + j;
+        const long long v = v0 + 16ll * s + 8 * h + l8;
+        if (s < steps && v < v1) {
+          int vb, z, y, x;
+          decode(v, vol, vb, z, y, x);
+          if (bok) rb[j][h] = *reinterpret_cast<const uint4*>(dZ.p + v * dZ.cs + dZ.co + 8 * oct);
+          z += dz; y += dy; x += dx;
+          if (rok && z >= 0 && z < vol.D && y >= 0 && y < vol.H && x >= 0 && x < vol.W) {
+            const long long sv = (((long long)vb * vol.D + z) * vol.H + y) * vol.W + x;
+            ra[j][h] = *reinterpret_cast<const uint4*>(X.p + sv * X.cs + X.co + k0);
+          }
+        }
+      }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int j = 0; j < kSub; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint4 a = transpose8(ra[j][h], l8);   // row: channel k0+l8, voxels 8h..8h+7 of the step
+        const uint4 b = transpose8(rb[j][h], l8);   // row: channel 8 oct + l8
+        char* ap = reinterpret_cast<char*>(sA + (buf * kSub + j) * 128 * 16);
+        *reinterpret_cast<uint4*>(ap + (oct * 2 + h) * 128 + l8 * 16) = a;
+        if (bok) {
+          char* bp = reinterpret_cast<char*>(sB + (buf * kSub + j) * N * 16);
+          *reinterpret_cast<uint4*>(bp + (oct * 2 + h) * 128 + l8 * 16) = b;
+        }
+      }
+  };
+  gather(0);
+  store(0);
+  unsigned phase[2] = {0, 0};
+  bool ok = true;
+  for (int q = 0; q < nst; ++q) {
+    const int buf = q & 1;
+    if (q + 1 < nst) gather(q + 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < kSub; ++j) {
+        const int s = q * kSub + j;
+        if (s < steps) {
+          const unsigned long long ad = smem_desc(sA + (buf * kSub + j) * 128 * 16, 128, 256);
+          const unsigned long long bd = smem_desc(sB + (buf * kSub + j) * N * 16, 128, 256);
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                       :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(s > 0 ? 1u : 0u) : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   :: "r"(smem_addr(&bar[buf])) : "memory");
+    }
+    if (q + 1 < nst) {
+      const int nb = buf ^ 1;
+      if (q >= 1) {   // stage nb was last read by the MMAs of stage q - 1
+        ok = __syncthreads_and(mbar_wait(&bar[nb], phase[nb], 1 << 20)) != 0;
+        phase[nb] ^= 1;
+        if (!ok) break;
+      }
+      store(nb);
+    }
+  }
+  if (t == 0)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_addr(&bar[2])) : "memory");
+  bool done = __syncthreads_and(mbar_wait(&bar[2], 0, 1 << 20)) != 0;
+  if (ok && done) {
+    for (int q = nst >= 2 ? nst - 2 : 0; q < nst; ++q) {
+      const int b = q & 1;
+      done = __syncthreads_and(mbar_wait(&bar[b], phase[b], 1 << 20)) != 0 && done;
+      phase[b] ^= 1;
+    }
+  }
+  if (!ok || !done) {
+    if (t == 0) atomicExch(err, 1);
+    mbar_wait(&bar[2], 0, 1 << 20);   // let the issued MMAs finish before freeing the columns
+  } else if (steps > 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int R = blockIdx.x * 128 + t;   // this thread's accumulator row (lane t of tensor memory)
+#pragma unroll
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      unsigned r[16];
+      const unsigned addr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                     "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                     "=r"(r[14]), "=r"(r[15])
+                   : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (R < rows) {
+        const int tp = R / K, k = R % K;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) atomicAdd(&dW[((size_t)(c0 + c) * 27 + tp) * K + k], __uint_as_float(r[c]));
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kCols));
+}
+
+// dW[n][tap][k] += sum_v dZ[v][n] * X[v + off(tap)][k]   (FP32, CUDA cores): the
+// reference form of k_wgrad_tc, kept for the gradient check of the tensor-core form.
 // grid: (voxel chunks, 27 taps); each block reduces kWgTile voxels at a time through
 // shared memory and adds its partial sums to dW with atomics.
 constexpr int kWgTile = 32;
@@ -474,7 +672,34 @@ void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const fl
   }
 }
 
-void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW) {
+template <int N>
+void launch_wgrad_tc(cudaStream_t st, const Vol& vol, Act dZ, Act X, int K, float* dW, int* err) {
+  constexpr size_t smem = wgrad_smem_bytes<N>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_wgrad_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  const long long M = vol.voxels();
+  const int rowblocks = (27 * K + 127) / 128;
+  // about two blocks per SM: split the voxels into chunks of whole stages (64 voxels)
+  long long chunks = std::max(1ll, std::min((304ll + rowblocks - 1) / rowblocks, (M + 255) / 256));
+  long long chunk = (M + chunks - 1) / chunks;
+  chunk = (chunk + 63) / 64 * 64;
+  chunks = (M + chunk - 1) / chunk;
+  k_wgrad_tc<N><<<dim3((unsigned)rowblocks, (unsigned)chunks), 128, smem, st>>>(vol, dZ, X, K, dW, chunk, err);
+}
+
+void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW, int* err) {
+  switch (N) {
+    case 16: launch_wgrad_tc<16>(st, vol, dZ, X, K, dW, err); break;
+    case 32: launch_wgrad_tc<32>(st, vol, dZ, X, K, dW, err); break;
+    case 64: launch_wgrad_tc<64>(st, vol, dZ, X, K, dW, err); break;
+    default: wgrad_cuda_cores(st, vol, dZ, N, X, K, dW); break;
+  }
+}
+
+void wgrad_cuda_cores(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW) {
   const long long M = vol.voxels();
   const long long chunk = 4096;
   dim3 grid((unsigned)((M + chunk - 1) / chunk), 27);

@@ -73,6 +73,7 @@ struct ib3d_net {
   float* ds_t = nullptr;   // [patch][S^3]
   double* d_loss = nullptr;
   int* d_err = nullptr;    // set by a convolution whose tensor-core wait gave up
+  bool wgrad_cuda_cores = false;   // weight gradients on the CUDA cores (the tensor-core form's reference)
 };
 
 namespace {
@@ -172,7 +173,8 @@ void conv_bwd(ib3d_net* n, int l, const Vol& v, Act X, Act Y, Act gY, Act gX) {
   const long long M = v.voxels();
   relu_bwd(n->st, M, ly.N, gY, Y);
   bias_grad(n->st, M, gY, ly.N, n->g + ly.b);
-  wgrad(n->st, v, gY, ly.N, X, ly.K, n->g + ly.w);
+  if (n->wgrad_cuda_cores) wgrad_cuda_cores(n->st, v, gY, ly.N, X, ly.K, n->g + ly.w);
+  else wgrad(n->st, v, gY, ly.N, X, ly.K, n->g + ly.w, n->d_err);
   if (gX.p) conv(n->st, v, gY, ly.N, wt(n, l), nullptr, 0, -1, gX, ly.K, n->d_err);
 }
 
@@ -513,6 +515,12 @@ int ib3d_net_set_coarsening(ib3d_net* n, int f) {
   if (!n || (f != 1 && f != 2 && f != 4)) return IB3D_ERR_ARG;
   n->coarsen = f;
   n->count = 0;
+  return IB3D_OK;
+}
+
+int ib3d_net_set_wgrad_tensor_cores(ib3d_net* n, int on) {
+  if (!n) return IB3D_ERR_ARG;
+  n->wgrad_cuda_cores = on == 0;
   return IB3D_OK;
 }
 

@@ -26,7 +26,10 @@ struct Act {
 // device misbehaves); the host checks it after synchronising
 void conv(cudaStream_t st, const Vol& vol, Act X, int K, const bf16* W, const float* bias, int relu, int sign, Act Y,
           int N, int* err);
-void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW);
+// weight gradients on the tensor cores (k_wgrad_tc; err as for conv), and the FP32
+// CUDA-core form kept as its reference
+void wgrad(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW, int* err);
+void wgrad_cuda_cores(cudaStream_t st, const Vol& vol, Act dZ, int N, Act X, int K, float* dW);
 void bias_grad(cudaStream_t st, long long M, Act dZ, int N, float* db);
 void relu_bwd(cudaStream_t st, long long M, int C, Act dY, Act Y);
 void pool_fwd(cudaStream_t st, const Vol& out, int C, Act in, Act o);

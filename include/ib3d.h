@@ -340,6 +340,10 @@ int ib3d_net_capture(ib3d_net* net, ib3d_ctx* ctx, int npatches, uint64_t seed);
  * inference use the same f; changing it clears the training set. */
 int ib3d_net_set_coarsening(ib3d_net* net, int f);
 int ib3d_net_train(ib3d_net* net, int steps, int batch, double lr, uint64_t seed, double* last_loss);
+/* Weight gradients of the convolutions: on the tensor cores (on != 0, the default:
+ * an implicit GEMM over the voxels with tcgen05.mma) or on the CUDA cores in FP32
+ * (on == 0, the reference the tensor-core form is checked against). */
+int ib3d_net_set_wgrad_tensor_cores(ib3d_net* net, int on);
 /* Keeps the two previous pressures and the previous correction's residual in ctx
  * (needed by capture and by the learned warm start); ib3d_attach_net calls it. */
 int ib3d_enable_history(ib3d_ctx* ctx);

@@ -91,6 +91,37 @@ def compare(grad, ref, rel_max, cos_min, label):
         assert rel < rel_max and cos > cos_min, (label, l, what, rel, cos)
 
 
+def test_tensor_core_weight_gradients_match_the_cuda_core_reduction(ib3d):
+    """The weight gradients of the implicit-GEMM tcgen05 kernel (k_wgrad_tc) against
+    the FP32 CUDA-core reduction on the same batch: both sum the same BF16 products in
+    FP32, in different orders, so every weight block must agree to accumulation
+    rounding (relative norm 1e-4); the loss, bias and head gradients do not depend on
+    the kernel (their atomic sums may still round differently: 1e-6)."""
+    net = ib3d.Net(seed=3)
+    lay, head = layout()
+    rng = np.random.default_rng(4)
+    B, S = 2, 16
+    x = rng.standard_normal((B, S, S, S, 4)).astype(np.float32)
+    t = rng.standard_normal((B, S, S, S)).astype(np.float32)
+    params = net.get_params()
+    params[head:head + 16] = rng.standard_normal(16) * 0.3
+    net.set_params(params)
+    loss_tc, g_tc, _ = net.loss_grad(x, t)
+    net.set_wgrad_tensor_cores(False)
+    loss_cc, g_cc, _ = net.loss_grad(x, t)
+    net.set_wgrad_tensor_cores(True)
+    assert abs(loss_tc - loss_cc) <= 1e-6 * loss_cc
+    close = lambda a, c: np.linalg.norm(a - c) <= 1e-6 * np.linalg.norm(c) + 1e-30
+    for l, (w, b, n, k) in enumerate(lay):
+        gt, gc = g_tc[w:b], g_cc[w:b]
+        rel = np.linalg.norm(gt - gc) / np.linalg.norm(gc)
+        print(f"layer {l} ({n}x{k}): weight gradient rel {rel:.2e}")
+        assert rel < 1e-4, (l, rel)
+        assert close(g_tc[b:b + n], g_cc[b:b + n]), l
+    assert close(g_tc[head:head + 17], g_cc[head:head + 17])
+    net.close()
+
+
 def test_net_loss_and_gradients_match_float64_reference(ib3d):
     """Loss and every parameter gradient of one batch. Against the float64 network
     with the library's BF16 roundings the differences come only from FP32 against
