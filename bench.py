@@ -133,14 +133,19 @@ def load_net(pkg, name: str = "", coarsen: int = 4):
 
 
 def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200.0, 250.0, 300.0, 350.0),
-              steps: int = 24, patches: int = 8, init: str = "", lr0: float = 1e-3) -> dict:
+              steps: int = 24, patches: int = 8, init: str = "", lr0: float = 1e-3, windows=None,
+              eval_spinup: int = 0) -> dict:
     """Generates snapshots (perturbed runs at the given Reynolds numbers -- by default
     Re 200/250/300/350 --, `steps` steps each, `patches` random patches of 128^3 cells
     per step from step 3), trains with Adam for `seconds` (batch 8, lr 1e-3 then 2e-4
     for the last 30 %), writes the FP32 weights, and compares sweeps on a held-out Re
     275 run (adaptive pass lengths, so that the counts resolve differences below 256
     sweeps). With `init` the training starts from those weights (a networks.json name or
-    a path), at learning rate lr0 (then lr0/5 for the last 30 %)."""
+    a path), at learning rate lr0 (then lr0/5 for the last 30 %). With `windows` the
+    patches come from those step windows of each run ((first, last), 1-based; runs go
+    on to the last window's end, so later windows see the developed wake), and with
+    `eval_spinup` the held-out run is also compared on a developed wake after that
+    many steps."""
     import dataclasses
     import numpy as np
     learned = importlib.import_module("ib3d_gpu_gb300.learned")
@@ -148,9 +153,13 @@ def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200
     if net is None:
         net = pkg.Net(seed=0)
     net.set_coarsening(coarsen)
-    net.reserve(128 // coarsen, len(reynolds) * (steps - 2) * patches)     # patches of 128^3 cells
+    per_run = sum(b - a + 1 for a, b in windows) if windows else steps - 2
+    net.reserve(128 // coarsen, len(reynolds) * per_run * patches)     # patches of 128^3 cells
     net.coarsen = coarsen
-    gen = learned.generate(net, cs, list(reynolds), steps, patches)
+    if windows:
+        gen = learned.generate_windows(net, cs, list(reynolds), windows, patches)
+    else:
+        gen = learned.generate(net, cs, list(reynolds), steps, patches)
     fit = lambda: float(np.mean([net.train(1, batch=8, lr=0.0, seed=10 ** 6 + q) for q in range(16)]))
     before = fit()
     t0, steps = time.perf_counter(), 0
@@ -161,11 +170,23 @@ def train_net(pkg, cs, out: str, seconds: float, coarsen: int = 2, reynolds=(200
     after = fit()
     pathlib.Path(out).parent.mkdir(parents=True, exist_ok=True)
     net.get_params().astype("<f4").tofile(out)
+    t_train = time.perf_counter() - t0
     ev = learned.evaluate(net, dataclasses.replace(cs), 275.0, 12, inner_schedule=1)
-    return {"weights": str(out), "patches": gen["patches"], "generate_s": gen["seconds"], "adam_steps": steps,
-            "train_s": time.perf_counter() - t0, "training_set_loss": [before, after],
-            "eval_re275": {k: {"sweeps": v["sweeps"], "seconds": v["seconds"], "initial_err": v["initial_err"]}
-                           for k, v in ev.items()}}
+    res = {"weights": str(out), "patches": gen["patches"], "generate_s": gen["seconds"], "adam_steps": steps,
+           "train_s": t_train, "training_set_loss": [before, after],
+           "eval_re275": {k: {"sweeps": v["sweeps"], "seconds": v["seconds"], "initial_err": v["initial_err"]}
+                          for k, v in ev.items()}}
+    if eval_spinup:
+        fd, path = tempfile.mkstemp(suffix=".ib3drst")
+        os.close(fd)
+        try:
+            dev = learned.evaluate_developed(net, dataclasses.replace(cs), 275.0, eval_spinup, 12, path,
+                                             inner_schedule=1)
+        finally:
+            os.unlink(path)
+        res["eval_re275_developed"] = {k: {"sweeps": v["sweeps"]} for k, v in dev.items()}
+        res["eval_re275_developed"]["spinup"] = eval_spinup
+    return res
 
 
 def train_moving(pkg, cs, out: str, seconds: float, weights: str = "", coarsen: int = 4, steps: int = 200,
@@ -773,6 +794,11 @@ def main():
     ap.add_argument("--train-steps", type=int, default=24, help="steps of each --train-net run")
     ap.add_argument("--train-patches", type=int, default=8, help="patches captured per step by --train-net")
     ap.add_argument("--train-init", default="", help="weights --train-net starts from (default: random)")
+    ap.add_argument("--train-windows", default="",
+                    help="--train-net: comma-separated step windows first-last whose steps are captured "
+                         "(default: steps 3..--train-steps)")
+    ap.add_argument("--eval-spinup", type=int, default=0,
+                    help="--train-net: also compare the warm starts on held-out Re 275 after this many steps")
     ap.add_argument("--train-lr", type=float, default=1e-3, help="--train-net's learning rate (then a fifth)")
     ap.add_argument("--weights", default="", help="weights file in ib3d-gpu_gb300/weights (default: networks.json's)")
     ap.add_argument("--moving", action="store_true",
@@ -797,10 +823,12 @@ def main():
     arms = set(args.arms.split(","))
     if args.train_net:
         if dist.rank == 0:
+            windows = [tuple(int(x) for x in w.split("-")) for w in args.train_windows.split(",")] \
+                if args.train_windows else None
             print(json.dumps(train_net(pkg, workload(pkg, args.case), args.train_net, args.train_seconds,
                                        args.coarsen, [float(r) for r in args.train_re.split(",")],
                                        args.train_steps, args.train_patches, args.train_init,
-                                       args.train_lr)), flush=True)
+                                       args.train_lr, windows, args.eval_spinup)), flush=True)
         dist.close()
         return
     if args.train_moving:

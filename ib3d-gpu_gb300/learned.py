@@ -58,6 +58,53 @@ def generate(net: Net, cs, reynolds, steps: int, patches_per_step: int, first_ca
     return {"patches": net.dataset_size(), "seconds": time.perf_counter() - t0, "sweeps": sweeps}
 
 
+def generate_windows(net: Net, cs, reynolds, windows, patches_per_step: int, seed: int = 0, **opts) -> dict:
+    """Runs cs at each Reynolds number from the impulsive start to the end of the last
+    window and captures patches of every step inside the windows ((first, last) step
+    numbers, 1-based): the transient after the start and the developed wake later on."""
+    t0 = time.perf_counter()
+    last = max(b for _, b in windows)
+    sweeps = []
+    for re in reynolds:
+        s = perturbed_run(cs, re, seed=int(re) + seed, **solver_options(warm_start=WARM_PREV, **opts))
+        s.enable_history()
+        for q in range(1, last + 1):
+            st, _ = s.step(q == 1)
+            if any(a <= q <= b for a, b in windows):
+                sweeps.append(st["sweeps"])
+                net.capture(s, patches_per_step, seed=1000 * int(re) + q + seed)
+        s.close()
+    return {"patches": net.dataset_size(), "seconds": time.perf_counter() - t0, "sweeps": sweeps}
+
+
+def evaluate_developed(net: Net, cs, re: float, spinup: int, steps: int, path: str, seed: int = 7,
+                       **opts) -> dict:
+    """Held-out run at re spun up for `spinup` steps (previous-correction warm start)
+    and saved to the restart file `path`; then both warm starts continue from it for
+    `steps` steps. The first two steps after the restart have no history for the
+    network (both arms then start from zero and from the previous correction), so the
+    comparison is over the steps after them."""
+    s = perturbed_run(cs, re, seed=seed, **solver_options(warm_start=WARM_PREV, **opts))
+    for q in range(1, spinup + 1):
+        s.step(q == 1)
+    s.write_restart(path, totime=spinup * cs.dt, ita=spinup, ita1=spinup)
+    s.close()
+    out = {}
+    for name, mode in (("prev", WARM_PREV), ("learned", WARM_LEARNED)):
+        s = setup_case(dataclasses.replace(cs, re=re), **solver_options(warm_start=mode, **opts))
+        if mode == WARM_LEARNED:
+            s.attach_net(net)
+        s.read_restart(path)
+        sw, coefs = [], []
+        for q in range(1, steps + 1):
+            st, coef = s.step(q == 1)
+            sw.append(st["sweeps"])
+            coefs.append(list(coef))
+        s.close()
+        out[name] = {"sweeps": sw, "coef": coefs}
+    return out
+
+
 def train(net: Net, steps: int, batch: int = 8, lr: float = 1e-3, chunk: int = 100, seed: int = 0) -> dict:
     """Adam steps in chunks (the loss of each chunk's last step is recorded)."""
     t0 = time.perf_counter()
