@@ -39,22 +39,23 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
   const float ax0[4] = {a0.x, a0.y, a0.z, a0.w};
   const float ax1[4] = {a1.x, a1.y, a1.z, a1.w};
   const float ax2[4] = {a2.x, a2.y, a2.z, a2.w};
+  // every cell is computed and a NaN right-hand side (a non-fluid cell, or the row's
+  // padding) selects the old value, so the four updates run without branches
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const float r = rv[c];
-    if (r == r) {   // fluid cell (NaN marks the others, including the row's padding)
-      const float W = FIRST ? ox[c] : ox[c + 1];
-      const float E = FIRST ? ox[c + 1] : ox[c + 2];
-      float num = r;
-      num = fmaf(-ax0[c], W, num);
-      num = fmaf(-ax2[c], E, num);
-      num = fmaf(-ay0, sv[c], num);
-      num = fmaf(-ay2, nv[c], num);
-      num = fmaf(-az0, bv[c], num);
-      num = fmaf(-az2, tv[c], num);
-      const float diag = ax1[c] + ay1 + az1;
-      ev[c] = sor32_update(ev[c], num, diag, omega, om1);
-    }
+    const float W = FIRST ? ox[c] : ox[c + 1];
+    const float E = FIRST ? ox[c + 1] : ox[c + 2];
+    float num = r;
+    num = fmaf(-ax0[c], W, num);
+    num = fmaf(-ax2[c], E, num);
+    num = fmaf(-ay0, sv[c], num);
+    num = fmaf(-ay2, nv[c], num);
+    num = fmaf(-az0, bv[c], num);
+    num = fmaf(-az2, tv[c], num);
+    const float diag = ax1[c] + ay1 + az1;
+    const float upd = sor32_update(ev[c], num, diag, omega, om1);
+    ev[c] = r == r ? upd : ev[c];
   }
 }
 
