@@ -256,7 +256,7 @@ bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
          (p->precision >= IB3D_PREC_FP64 && p->precision <= IB3D_PREC_FP64_FAST) && (p->warm_start >= 0 && p->warm_start <= 2) &&
-         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel >= 0 && p->sweep_kernel <= 2) &&
+         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel >= 0 && p->sweep_kernel <= 3) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
          (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 && p->ramp_sweeps >= 0 &&
          (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&

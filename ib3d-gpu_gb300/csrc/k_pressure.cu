@@ -474,7 +474,7 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   const float om = (float)wi, om1 = (float)(1.0 - wi);
   const int inner = P.inner_sweeps < 1 ? 1 : P.inner_sweeps;
   const bool fused = P.sweep_kernel == 2;
-  const bool packed = (P.sweep_kernel == 0 || fused) && c->ep[0] != nullptr;
+  const bool packed = (P.sweep_kernel == 0 || P.sweep_kernel == 3 || fused) && c->ep[0] != nullptr;
   if (fused) {
     if (!packed || !fused_sweep_fits(d.nx)) {
       c->err = "sweep_kernel 2 (fused sweep) needs an even nx whose packed rows fit its blocks (nx <= 512)";

@@ -72,10 +72,18 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
 // warps that fit hide the load latency better than a longer unroll would.
 // Offsets are 32-bit (a packed array holds fewer than 2^31 entries, checked at
 // allocation).
+//
+// ALL_LOAD: lanes past the end of a row (when the row's groups do not fill whole
+// warps) load the row's last group instead of skipping their loads, and skip only the
+// store, so no branch guards the loads. The compiler then schedules the plane's loads
+// earlier, which costs registers (a few spill at the 64-register cap) but keeps more
+// bytes in flight: 5 % faster on arrays larger than L2 (384x256x256: 81.9 against 86.0
+// us per sweep), 6 % slower where they sit in L2 (256x192x192: 24.4 against 23.0), so
+// the launcher picks it by the arrays' size. Both forms give the same bits.
 constexpr int kPlanes = 8;
 constexpr int kRows = 4;
 
-template <int COLOR>
+template <int COLOR, bool ALL_LOAD>
 __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, const float* __restrict__ r_own,
                                                           float* __restrict__ e_own, const float* __restrict__ e_oth,
                                                           int Lp, float omega, float om1) {
@@ -89,13 +97,15 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
   const int k0 = blockIdx.z * kPlanes + 2;
   if (j <= d.ny + 1) {   // uniform across the warp, so the shuffles see all lanes
     const bool active = q < nq;
+    const bool lds = ALL_LOAD || active;                // this lane loads
+    const int qa = ALL_LOAD && !active ? nq - 1 : q;   // the group it loads
     const bool load_left = lane == 0, load_right = lane == 31 || q + 1 >= nq;
     const int plane = (d.ny + 2) * Lp;
-    const int sj = (j - 1) * Lp + 4 * q + 4;
+    const int sj = (j - 1) * Lp + 4 * qa + 4;
     const float ay0 = g.acy32[0][j - 1], ay1 = g.acy32[1][j - 1], ay2 = g.acy32[2][j - 1];
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 ob = active ? *reinterpret_cast<const float4*>(e_oth + (k0 - 2) * plane + sj) : z4;
-    float4 ox = active ? *reinterpret_cast<const float4*>(e_oth + (k0 - 1) * plane + sj) : z4;
+    float4 ob = lds ? *reinterpret_cast<const float4*>(e_oth + (k0 - 2) * plane + sj) : z4;
+    float4 ox = lds ? *reinterpret_cast<const float4*>(e_oth + (k0 - 1) * plane + sj) : z4;
 #pragma unroll
     for (int kk = 0; kk < kPlanes; ++kk) {
       const int k = k0 + kk;
@@ -104,7 +114,7 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
       // does this row start (i = 2) with the colour being updated?
       const bool own_first = (COLOR == 0) == (((j + k) & 1) == 1);
       float4 rr = z4, eo = z4, os = z4, on = z4, ot = z4;
-      if (active) {
+      if (lds) {
         rr = *reinterpret_cast<const float4*>(r_own + s0);
         eo = *reinterpret_cast<const float4*>(e_own + s0);
         os = *reinterpret_cast<const float4*>(e_oth + s0 - Lp);
@@ -113,8 +123,8 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
       }
       float left = __shfl_up_sync(0xffffffffu, ox.w, 1);
       float right = __shfl_down_sync(0xffffffffu, ox.x, 1);
-      if (active && load_left) left = e_oth[s0 - 1];
-      if (active && load_right) right = e_oth[s0 + 4];
+      if (lds && load_left) left = e_oth[s0 - 1];
+      if (lds && load_right) right = e_oth[s0 + 4];
       const float oxa[6] = {left, ox.x, ox.y, ox.z, ox.w, right};
       const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
       const float sv[4] = {os.x, os.y, os.z, os.w};
@@ -123,14 +133,14 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
       const float tv[4] = {ot.x, ot.y, ot.z, ot.w};
       float ev[4] = {eo.x, eo.y, eo.z, eo.w};
       const float az0 = g.acz32[0][k - 1], az1 = g.acz32[1][k - 1], az2 = g.acz32[2][k - 1];
-      if (active) {
+      if (lds) {
         const int sp = own_first ? 0 : 1;
-        const float4 a0 = g.axp[sp][0][q], a1 = g.axp[sp][1][q], a2 = g.axp[sp][2][q];
+        const float4 a0 = g.axp[sp][0][qa], a1 = g.axp[sp][1][qa], a2 = g.axp[sp][2][qa];
         if (own_first)
           update4<true>(rv, ev, oxa, sv, nv, bv, tv, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
         else
           update4<false>(rv, ev, oxa, sv, nv, bv, tv, a0, a1, a2, ay0, ay1, ay2, az0, az1, az2, omega, om1);
-        *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+        if (active) *reinterpret_cast<float4*>(e_own + s0) = make_float4(ev[0], ev[1], ev[2], ev[3]);
       }
       ob = ox;
       ox = ot;
@@ -448,10 +458,17 @@ void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   const float* r = c->rp[color];
   float* e = c->ep[color];
   const float* o = c->ep[1 - color];
-  if (color == 0)
-    cudaLaunchKernelEx(&cfg, k_sor32p<0>, d, c->g, r, e, o, c->packed_lp, omega, om1);
-  else
-    cudaLaunchKernelEx(&cfg, k_sor32p<1>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+  // the loads without branches where the four packed arrays exceed 96 MB of the 129 MB
+  // L2 (or when sweep_kernel 3 asks for them)
+  const size_t packed = 4 * sizeof(float) * (size_t)c->packed_lp * (size_t)d.NY2 * (size_t)d.NZ2;
+  const bool all_load = c->prm.sweep_kernel == 3 || (c->prm.sweep_kernel == 0 && packed > ((size_t)96 << 20));
+  if (all_load) {
+    if (color == 0) cudaLaunchKernelEx(&cfg, k_sor32p<0, true>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+    else cudaLaunchKernelEx(&cfg, k_sor32p<1, true>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+  } else {
+    if (color == 0) cudaLaunchKernelEx(&cfg, k_sor32p<0, false>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+    else cudaLaunchKernelEx(&cfg, k_sor32p<1, false>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+  }
 }
 
 // Rows per block and stages of the staged sweep for a row of nq float4 groups: 16 rows

@@ -200,10 +200,11 @@ def test_mixed_precision_matches_fp64_drag(ib3d, grids):
     s64.close(); s32.close()
 
 
-@pytest.mark.parametrize("name,kernel", [("tiny", 0), ("small", 0), ("tiny", 2), ("small", 2)])
+@pytest.mark.parametrize("name,kernel", [("tiny", 0), ("small", 0), ("tiny", 2), ("small", 2), ("small", 3)])
 def test_packed_fp32_sweep_matches_padded_layout(ib3d, grids, name, kernel):
-    """The FP32 sweep on colour-packed arrays (two colour passes, kernel 0, or one
-    fused z-wavefront launch per sweep, kernel 2) performs the same red-then-black
+    """The FP32 sweep on colour-packed arrays (two colour passes, kernel 0; the same with
+    its loads free of branches, kernel 3; or one fused z-wavefront launch per sweep,
+    kernel 2) performs the same red-then-black
     update with the same FP32 operation order as the sweep on the padded field
     layout, so whole mixed-precision steps agree bit for bit."""
     cs = grids.case(name)
