@@ -360,11 +360,18 @@ __device__ __forceinline__ void finish_block(SolveCtl* ctl, unsigned long long* 
 }
 
 // The FP32 SOR update shared by every FP32 sweep kernel: e <- (1-omega) e +
-// omega num / diag, the quotient through the hardware reciprocal (two
-// instructions instead of the IEEE division's sequence). The FP32 sweeps only
-// precondition the FP64 defect correction, whose FP64 residual decides
-// convergence, so the quotient's last-bit rounding does not reach the result.
+// omega num / diag, the quotient as a product with the hardware's approximate
+// reciprocal (rcp.approx.ftz.f32, one instruction) instead of the IEEE division's
+// sequence. diag is the sum of three positive Poisson diagonal entries, a normal
+// number far from the range limits, so the reciprocal needs no range handling. The
+// FP32 sweeps only precondition the FP64 defect correction, whose FP64 residual
+// decides convergence, so the quotient's last-bit rounding does not reach the result.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 __device__ __forceinline__ float sor32_update(float e, float num, float diag, float omega, float om1) {
-  return fmaf(om1, e, __fdividef(omega * num, diag));
+  return fmaf(om1, e, (omega * num) * rcp_approx(diag));
 }
 }  // namespace ib3d
