@@ -507,6 +507,9 @@ void ib3d_destroy(ib3d_ctx* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  for (cudaStream_t x : c->xfer)
+    if (x) cudaStreamDestroy(x);
+  if (c->xfer_ready) cudaEventDestroy(c->xfer_ready);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -694,9 +697,24 @@ int ib3d_download_fields(ib3d_ctx* c, double* u, double* v, double* w, double* u
   const size_t bytes = (size_t)c->d.n3 * sizeof(double);
   double* dst[7] = {u, v, w, ut, vt, wt, p};
   const double* src[7] = {c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p};
+  // the copies go round-robin over the context's stream and three more, which start
+  // once the work queued on the context's stream is done, so that several copy engines
+  // share the host link; the call returns when all of them have landed
+  if (!c->xfer_ready) {
+    IB3D_CUDA(c, cudaEventCreateWithFlags(&c->xfer_ready, cudaEventDisableTiming));
+    for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  }
+  IB3D_CUDA(c, cudaEventRecord(c->xfer_ready, c->st));
+  for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamWaitEvent(x, c->xfer_ready, 0));
+  int n = 0;
   for (int q = 0; q < 7; ++q)
-    if (dst[q]) IB3D_CUDA(c, cudaMemcpyAsync(dst[q], src[q], bytes, cudaMemcpyDeviceToHost, c->st));
+    if (dst[q]) {
+      cudaStream_t s = n % 4 == 0 ? c->st : c->xfer[n % 4 - 1];
+      IB3D_CUDA(c, cudaMemcpyAsync(dst[q], src[q], bytes, cudaMemcpyDeviceToHost, s));
+      ++n;
+    }
   IB3D_CUDA(c, cudaStreamSynchronize(c->st));
+  for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamSynchronize(x));
   return IB3D_OK;
 }
 

@@ -110,6 +110,10 @@ struct ib3d_ctx {
   ib3d::Dims d;
   ib3d_params prm;
   cudaStream_t st = nullptr;
+  // streams the host transfers of ib3d_download_fields spread over (created on first
+  // use), and the event that orders them after the work on st
+  cudaStream_t xfer[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t xfer_ready = nullptr;
   int device = 0;
   std::string err;
 
