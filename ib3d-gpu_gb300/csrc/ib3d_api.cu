@@ -283,7 +283,8 @@ using namespace ib3d;
 // FP32 copies of the nine Poisson tables (each padded to 8 floats; off32[3*axis+col]
 // is each table's offset) and, for even nx, the x tables regrouped for the
 // colour-packed sweep: hp[((s*3 + col)*nq + g)*4 + e] = Acx(i-1, col) at
-// i = 2 + s + 8g + 2e (0 beyond the row).
+// i = 2 + s + 8g + 2e (0 beyond the row), columns 1 and 3 (col 0, 2) negated: the
+// sweep subtracts their products with fused multiply-adds, fma(-a, x, num).
 static void poisson32_host(const ib3d_ctx* c, std::vector<float>& h32, std::vector<size_t>& off32,
                            std::vector<float>& hp) {
   h32.clear(); off32.clear(); hp.clear();
@@ -302,7 +303,10 @@ static void poisson32_host(const ib3d_ctx* c, std::vector<float>& h32, std::vect
         for (int g = 0; g < nq; ++g)
           for (int e = 0; e < 4; ++e) {
             const long long i = 2 + s + 8ll * g + 2 * e;
-            if (i <= nx + 1) hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = (float)c->hac[0][q][i - 1];
+            if (i <= nx + 1) {
+              const float a = (float)c->hac[0][q][i - 1];
+              hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = q == 1 ? a : -a;
+            }
           }
   }
 }

@@ -44,7 +44,8 @@ struct Grid1D {
   const float *acx32[3], *acy32[3], *acz32[3];
   // x coefficients regrouped for the colour-packed sweep: axp[s][c][q] holds column c
   // of Acx at the four cells i = (2+s) + 8q + {0,2,4,6} (s = 0 rows whose colour
-  // starts at i = 2, s = 1 at i = 3), as FP32 float4
+  // starts at i = 2, s = 1 at i = 3), as FP32 float4; columns c = 0 and 2 (the
+  // off-diagonal ones) are stored negated
   const float4* axp[2][3];
   // convection tables cc[fam][m], fam 0 uu,1 vv,2 ww,3 uv(=uw),4 vu(=vw),5 wu(=wv)
   const double* cc[6][12];

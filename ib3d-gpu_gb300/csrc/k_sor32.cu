@@ -27,9 +27,41 @@ namespace ib3d {
 // groups, plus 4 entries of left padding (ghost at 3) and 4 of right padding.
 int packed_row_length(int nx) { return 4 * (((nx >> 1) + 3) >> 2) + 8; }
 
-// Updates the four cells of one thread. FIRST: the row starts (i = 2) with the
-// colour being updated, so cell c's x neighbours are other-colour entries c-1 and c
-// (else c and c+1) of the row, ox[] holding entries -1..4.
+// Two FP32 values in one 64-bit register for the packed FP32 instructions of
+// sm_100 and later (fma/add/mul.rn.f32x2): each lane is rounded as the scalar
+// instruction rounds it (round to nearest, subnormals kept), so an update computed
+// on a pair has the bits of the two scalar updates, in half the instructions.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 v;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(lo), "f"(hi));
+  return v;
+}
+__device__ __forceinline__ void up2(f32x2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// Updates the four cells of one thread, as two pairs of cells. FIRST: the row
+// starts (i = 2) with the colour being updated, so cell c's x neighbours are
+// other-colour entries c-1 and c (else c and c+1) of the row, ox[] holding entries
+// -1..4. a0 and a2 hold the negated x off-diagonal coefficients (Grid1D::axp), so
+// fma(a0, W, num) is the scalar form's fma(-Acx(.,1), W, num); per cell the
+// operations and their order are those of the one-array kernel (k_sor32).
 template <bool FIRST>
 __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], const float (&ox)[6],
                                         const float (&sv)[4], const float (&nv)[4], const float (&bv)[4],
@@ -39,23 +71,29 @@ __device__ __forceinline__ void update4(const float (&rv)[4], float (&ev)[4], co
   const float ax0[4] = {a0.x, a0.y, a0.z, a0.w};
   const float ax1[4] = {a1.x, a1.y, a1.z, a1.w};
   const float ax2[4] = {a2.x, a2.y, a2.z, a2.w};
+  const f32x2 nay0 = pk2(-ay0, -ay0), nay2 = pk2(-ay2, -ay2), ay1p = pk2(ay1, ay1);
+  const f32x2 naz0 = pk2(-az0, -az0), naz2 = pk2(-az2, -az2), az1p = pk2(az1, az1);
+  const f32x2 om = pk2(omega, omega), om1p = pk2(om1, om1);
   // every cell is computed and a NaN right-hand side (a non-fluid cell, or the row's
   // padding) selects the old value, so the four updates run without branches
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const float r = rv[c];
-    const float W = FIRST ? ox[c] : ox[c + 1];
-    const float E = FIRST ? ox[c + 1] : ox[c + 2];
-    float num = r;
-    num = fmaf(-ax0[c], W, num);
-    num = fmaf(-ax2[c], E, num);
-    num = fmaf(-ay0, sv[c], num);
-    num = fmaf(-ay2, nv[c], num);
-    num = fmaf(-az0, bv[c], num);
-    num = fmaf(-az2, tv[c], num);
-    const float diag = ax1[c] + ay1 + az1;
-    const float upd = sor32_update(ev[c], num, diag, omega, om1);
-    ev[c] = r == r ? upd : ev[c];
+  for (int c = 0; c < 4; c += 2) {
+    const int w = FIRST ? c : c + 1;   // ox index of the first cell's W neighbour
+    f32x2 num = pk2(rv[c], rv[c + 1]);
+    num = fma2(pk2(ax0[c], ax0[c + 1]), pk2(ox[w], ox[w + 1]), num);
+    num = fma2(pk2(ax2[c], ax2[c + 1]), pk2(ox[w + 1], ox[w + 2]), num);
+    num = fma2(nay0, pk2(sv[c], sv[c + 1]), num);
+    num = fma2(nay2, pk2(nv[c], nv[c + 1]), num);
+    num = fma2(naz0, pk2(bv[c], bv[c + 1]), num);
+    num = fma2(naz2, pk2(tv[c], tv[c + 1]), num);
+    float d0, d1;
+    up2(add2(add2(pk2(ax1[c], ax1[c + 1]), ay1p), az1p), d0, d1);
+    // sor32_update on the pair: fma(om1, e, (omega * num) * rcp(diag))
+    const f32x2 q = mul2(mul2(om, num), pk2(rcp_approx(d0), rcp_approx(d1)));
+    float u0, u1;
+    up2(fma2(om1p, pk2(ev[c], ev[c + 1]), q), u0, u1);
+    ev[c] = rv[c] == rv[c] ? u0 : ev[c];
+    ev[c + 1] = rv[c + 1] == rv[c + 1] ? u1 : ev[c + 1];
   }
 }
 
