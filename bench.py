@@ -1016,7 +1016,7 @@ def main():
         "cells_per_s": value * ncell,
         "phase_ms_per_step": {p: tm[f"{p}_ms"] / args.steps for p in pkg.Timers.PHASES},
         "drag_lift": head["coef"],
-        "roofline": {"kernel": "k_sor32p (FP32 red-black sweep, colour-packed; one launch per colour pass)",
+        "roofline": {"kernel": "k_sor32p2 (FP32 red-black sweep, colour-packed, two rows per thread; one launch per colour pass)",
                      "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": DRAM_BYTES_PER_CELL_SWEEP32 * ncell * sweeps_per_launch,
                      "traffic_cold": DRAM_BYTES_PER_CELL_SWEEP32_COLD * ncell * sweeps_per_launch,

@@ -256,7 +256,7 @@ bool valid_params(const ib3d_params* p) {
   return p && p->re > 0 && std::isfinite(p->re) && p->deltat > 0 && std::isfinite(p->deltat) && p->omega > 0 &&
          p->omega < 2 && p->eps > 0 && p->max_sweeps >= 1 && (p->criterion == 0 || p->criterion == 1) &&
          (p->precision >= IB3D_PREC_FP64 && p->precision <= IB3D_PREC_FP64_FAST) && (p->warm_start >= 0 && p->warm_start <= 2) &&
-         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel >= 0 && p->sweep_kernel <= 3) &&
+         p->check_every >= 1 && p->inner_sweeps >= 1 && (p->sweep_kernel >= 0 && p->sweep_kernel <= 4) &&
          (p->omega_inner == 0.0 || (p->omega_inner > 0.0 && p->omega_inner < 2.0)) &&
          (p->inner_schedule >= IB3D_INNER_FIXED && p->inner_schedule <= IB3D_INNER_TAIL) && p->smooth_sweeps >= 0 && p->ramp_sweeps >= 0 &&
          (p->outlet == IB3D_OUTLET_ZERO_GRADIENT || p->outlet == IB3D_OUTLET_CONVECTIVE) &&
@@ -511,6 +511,7 @@ void ib3d_destroy(ib3d_ctx* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (cudaStream_t x : c->xfer)
     if (x) cudaStreamDestroy(x);
   if (c->xfer_ready) cudaEventDestroy(c->xfer_ready);

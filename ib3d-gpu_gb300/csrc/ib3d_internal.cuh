@@ -146,6 +146,13 @@ struct ib3d_ctx {
   // second pair of colour-packed corrections for the fused sweep (sweep_kernel 2): each
   // sweep reads ep[] and writes epn[], then the pairs swap
   float* epn[2] = {nullptr, nullptr};
+  // CUDA graph of kGraphSweeps FP32 sweeps of the colour-packed kernels (k_sor32.cu),
+  // with the tables, relaxation and kernel choice it was captured with
+  cudaGraphExec_t sweep_exec = nullptr;
+  ib3d::Grid1D sweep_g{};
+  float sweep_w = 0.f, sweep_w1 = 0.f;
+  int sweep_kern = -1;
+  bool sweep_graph_failed = false;   // capture refused once: the sweeps launch one by one
   int packed_lp = 0;
   unsigned char* cell = nullptr;
   int* ibmap = nullptr;
@@ -238,6 +245,8 @@ void launch_momentum_fast(ib3d_ctx* c, bool ab2);
 // k_sor32.cu
 int packed_row_length(int nx);
 void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1);
+void launch_sor32_sweep(ib3d_ctx* c, float omega, float om1);
+void run_sor32_sweeps(ib3d_ctx* c, int n, float omega, float om1);
 void launch_accumulate_packed(ib3d_ctx* c);
 void launch_sor32_fused(ib3d_ctx* c, float omega, float om1);
 bool fused_sweep_fits(int nx);

@@ -11,6 +11,7 @@
 // bit-identical to the serial oracle. Kernels address the reference's padded
 // Fortran layout directly and mask by the uint8 cell flags instead of gathering
 // through int64 index lists.
+#include <algorithm>
 #include <cmath>
 
 #include "ib3d_internal.cuh"
@@ -469,12 +470,11 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
   const ib3d_params& P = c->prm;
   const unsigned ncol = (unsigned)((((long long)d.nx + 1) / 2) * d.ny * d.nz);
   const unsigned gcol = (ncol + kBlock - 1) / kBlock;
-  const long long ncell = (long long)d.nx * d.ny * d.nz;
   const double wi = P.omega_inner > 0.0 ? P.omega_inner : P.omega;
   const float om = (float)wi, om1 = (float)(1.0 - wi);
   const int inner = P.inner_sweeps < 1 ? 1 : P.inner_sweeps;
   const bool fused = P.sweep_kernel == 2;
-  const bool packed = (P.sweep_kernel == 0 || P.sweep_kernel == 3 || fused) && c->ep[0] != nullptr;
+  const bool packed = P.sweep_kernel != 1 && c->ep[0] != nullptr;
   if (fused) {
     if (!packed || !fused_sweep_fits(d.nx)) {
       c->err = "sweep_kernel 2 (fused sweep) needs an even nx whose packed rows fit its blocks (nx <= 512)";
@@ -534,10 +534,13 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
       PhaseScope ps(c, PH_SOR32);
       c->launches += fused ? batch : 2 * batch;
       c->t_launches32 += fused ? batch : 2 * batch;
-      for (int q = 0; q < batch; ++q) {
-        // the solve's first sweeps run at relaxation 1 (smooth_sweeps: Gauss-Seidel damps the
-        // high-frequency error that the over-relaxed sweeps barely touch), the next
-        // ramp_sweeps with the relaxation rising linearly from 1 to omega_inner
+      // the solve's first sweeps run at relaxation 1 (smooth_sweeps: Gauss-Seidel damps the
+      // high-frequency error that the over-relaxed sweeps barely touch), the next
+      // ramp_sweeps with the relaxation rising linearly from 1 to omega_inner; the
+      // colour-packed kernels run the sweeps after those through run_sor32_sweeps
+      const int special = outer == 0 ? P.smooth_sweeps + P.ramp_sweeps : 0;
+      const int direct = packed && !fused ? std::min(batch, special) : batch;
+      for (int q = 0; q < direct; ++q) {
         const bool smooth = outer == 0 && q < P.smooth_sweeps;
         float w = smooth ? 1.0f : om, w1 = smooth ? 0.0f : om1;
         if (outer == 0 && q >= P.smooth_sweeps && q < P.smooth_sweeps + P.ramp_sweeps) {
@@ -548,13 +551,13 @@ int run_sor_fp32dc(ib3d_ctx* c, ib3d_solve_stats* st) {
         if (fused) {
           launch_sor32_fused(c, w, w1);
         } else if (packed) {
-          launch_sor32_packed(c, 0, w, w1);
-          launch_sor32_packed(c, 1, w, w1);
+          launch_sor32_sweep(c, w, w1);
         } else {
           k_sor32<0><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, w, w1);
           k_sor32<1><<<gcol, kBlock, 0, c->st>>>(d, c->g, c->r32, c->e32, c->cell, w, w1);
         }
       }
+      if (direct < batch) run_sor32_sweeps(c, batch - direct, om, om1);
     }
     {
       PhaseScope ps(c, PH_RESIDUAL);

@@ -17,6 +17,8 @@
 //
 // Per cell the arithmetic and its order are those of the one-array form (k_sor32
 // in k_pressure.cu), so both give the same bits.
+#include <algorithm>
+#include <cstring>
 #include <utility>
 
 #include "ib3d_internal.cuh"
@@ -185,6 +187,109 @@ __global__ void __launch_bounds__(32 * kRows, 8) k_sor32p(Dims d, Grid1D g, cons
     }
   }
   // the next pass may launch now; its griddepcontrol.wait still waits for this grid
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// One colour pass with two rows per thread. A warp owns rows a = j (even) and
+// b = j + 1 over kPlanes2 planes from an even plane k0, so the row phase of each
+// row at each plane is fixed by the colour: row a starts with the updated colour
+// at even planes exactly when COLOR is 1, row b at odd planes. The thread keeps
+// the x coefficients of both phases in registers for all its planes instead of
+// loading them per plane, and each row's other-colour centre values serve as the
+// other row's y neighbour, so a plane of two rows loads eight float4 groups
+// (r and e of both rows, the other colour at row a-1, row b+1 and both rows of
+// plane k+1) against ten plus six coefficient groups for two rows of k_sor32p.
+// Row b may be the top ghost row (odd ny): its other-colour values (zero) are
+// read as row a's neighbours, and its own update is neither loaded nor stored.
+// Per cell the arithmetic is update4's, so the bits are those of k_sor32p.
+constexpr int kRows2 = 4;
+constexpr int kPlanes2 = 8;
+static_assert(kPlanes2 % 2 == 0, "blocks start at even planes");
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+template <int COLOR>
+__global__ void __launch_bounds__(32 * kRows2, 4) k_sor32p2(Dims d, Grid1D g, const float* __restrict__ r_own,
+                                                                    float* __restrict__ e_own,
+                                                                    const float* __restrict__ e_oth, int Lp, float omega,
+                                                                    float om1) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int nq = ((d.nx >> 1) + 3) >> 2;
+  const int lane = threadIdx.x;
+  const int q = blockIdx.x * 32 + lane;
+  const int ja = blockIdx.y * (2 * kRows2) + 2 * threadIdx.y + 2;
+  const int k0 = blockIdx.z * kPlanes2 + 2;
+  if (ja <= d.ny + 1) {   // uniform across the warp, so the shuffles see all lanes
+    const bool lds = q < nq;
+    const bool rowb = ja + 1 <= d.ny + 1;
+    const bool load_left = lane == 0, load_right = lane == 31 || q + 1 >= nq;
+    const int plane = (d.ny + 2) * Lp;
+    const int sa = (ja - 1) * Lp + 4 * q + 4;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float ya0 = g.acy32[0][ja - 1], ya1 = g.acy32[1][ja - 1], ya2 = g.acy32[2][ja - 1];
+    const float yb0 = rowb ? g.acy32[0][ja] : 0.f, yb1 = rowb ? g.acy32[1][ja] : 0.f,
+                yb2 = rowb ? g.acy32[2][ja] : 0.f;
+    // P: the phase of row a at even planes (and of row b at odd ones); Q the other
+    const float4 p0 = lds ? g.axp[1 - COLOR][0][q] : z4, p1 = lds ? g.axp[1 - COLOR][1][q] : z4,
+                 p2 = lds ? g.axp[1 - COLOR][2][q] : z4;
+    const float4 q0 = lds ? g.axp[COLOR][0][q] : z4, q1 = lds ? g.axp[COLOR][1][q] : z4,
+                 q2 = lds ? g.axp[COLOR][2][q] : z4;
+    float4 oba = lds ? ld4(e_oth + (k0 - 2) * plane + sa) : z4, obb = lds ? ld4(e_oth + (k0 - 2) * plane + sa + Lp) : z4;
+    float4 oxa = lds ? ld4(e_oth + (k0 - 1) * plane + sa) : z4, oxb = lds ? ld4(e_oth + (k0 - 1) * plane + sa + Lp) : z4;
+#pragma unroll
+    for (int kk = 0; kk < kPlanes2; ++kk) {
+      const int k = k0 + kk;
+      if (k > d.nz + 1) break;
+      const int s0 = (k - 1) * plane + sa;
+      float4 ra = z4, ea = z4, rb = z4, eb = z4, osa = z4, onb = z4, ota = z4, otb = z4;
+      if (lds) {
+        ra = ld4(r_own + s0);
+        ea = ld4(e_own + s0);
+        osa = ld4(e_oth + s0 - Lp);
+        ota = ld4(e_oth + s0 + plane);
+        otb = ld4(e_oth + s0 + Lp + plane);
+        if (rowb) {
+          rb = ld4(r_own + s0 + Lp);
+          eb = ld4(e_own + s0 + Lp);
+          onb = ld4(e_oth + s0 + 2 * Lp);
+        }
+      }
+      float la = __shfl_up_sync(0xffffffffu, oxa.w, 1), ra_ = __shfl_down_sync(0xffffffffu, oxa.x, 1);
+      float lb = __shfl_up_sync(0xffffffffu, oxb.w, 1), rb_ = __shfl_down_sync(0xffffffffu, oxb.x, 1);
+      if (lds && load_left) {
+        la = e_oth[s0 - 1];
+        lb = e_oth[s0 + Lp - 1];
+      }
+      if (lds && load_right) {
+        ra_ = e_oth[s0 + 4];
+        rb_ = e_oth[s0 + Lp + 4];
+      }
+      const float z0 = g.acz32[0][k - 1], z1 = g.acz32[1][k - 1], z2 = g.acz32[2][k - 1];
+      if (lds) {
+        const float xa[6] = {la, oxa.x, oxa.y, oxa.z, oxa.w, ra_};
+        const float xb[6] = {lb, oxb.x, oxb.y, oxb.z, oxb.w, rb_};
+        const float rva[4] = {ra.x, ra.y, ra.z, ra.w}, rvb[4] = {rb.x, rb.y, rb.z, rb.w};
+        const float sva[4] = {osa.x, osa.y, osa.z, osa.w}, nva[4] = {oxb.x, oxb.y, oxb.z, oxb.w};
+        const float svb[4] = {oxa.x, oxa.y, oxa.z, oxa.w}, nvb[4] = {onb.x, onb.y, onb.z, onb.w};
+        const float bva[4] = {oba.x, oba.y, oba.z, oba.w}, tva[4] = {ota.x, ota.y, ota.z, ota.w};
+        const float bvb[4] = {obb.x, obb.y, obb.z, obb.w}, tvb[4] = {otb.x, otb.y, otb.z, otb.w};
+        float eva[4] = {ea.x, ea.y, ea.z, ea.w}, evb[4] = {eb.x, eb.y, eb.z, eb.w};
+        if ((kk & 1) == 0) {
+          update4<COLOR != 0>(rva, eva, xa, sva, nva, bva, tva, p0, p1, p2, ya0, ya1, ya2, z0, z1, z2, omega, om1);
+          update4<COLOR == 0>(rvb, evb, xb, svb, nvb, bvb, tvb, q0, q1, q2, yb0, yb1, yb2, z0, z1, z2, omega, om1);
+        } else {
+          update4<COLOR == 0>(rva, eva, xa, sva, nva, bva, tva, q0, q1, q2, ya0, ya1, ya2, z0, z1, z2, omega, om1);
+          update4<COLOR != 0>(rvb, evb, xb, svb, nvb, bvb, tvb, p0, p1, p2, yb0, yb1, yb2, z0, z1, z2, omega, om1);
+        }
+        *reinterpret_cast<float4*>(e_own + s0) = make_float4(eva[0], eva[1], eva[2], eva[3]);
+        if (rowb) *reinterpret_cast<float4*>(e_own + s0 + Lp) = make_float4(evb[0], evb[1], evb[2], evb[3]);
+      }
+      oba = oxa;
+      oxa = ota;
+      obb = oxb;
+      oxb = otb;
+    }
+  }
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
@@ -496,17 +601,109 @@ void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
   const float* r = c->rp[color];
   float* e = c->ep[color];
   const float* o = c->ep[1 - color];
-  // the loads without branches where the four packed arrays exceed 96 MB of the 129 MB
-  // L2 (or when sweep_kernel 3 asks for them)
-  const size_t packed = 4 * sizeof(float) * (size_t)c->packed_lp * (size_t)d.NY2 * (size_t)d.NZ2;
-  const bool all_load = c->prm.sweep_kernel == 3 || (c->prm.sweep_kernel == 0 && packed > ((size_t)96 << 20));
-  if (all_load) {
+  // the loads without branches (sweep_kernel 0 beyond L2, and 3) or behind branches (4)
+  if (c->prm.sweep_kernel != 4) {
     if (color == 0) cudaLaunchKernelEx(&cfg, k_sor32p<0, true>, d, c->g, r, e, o, c->packed_lp, omega, om1);
     else cudaLaunchKernelEx(&cfg, k_sor32p<1, true>, d, c->g, r, e, o, c->packed_lp, omega, om1);
   } else {
     if (color == 0) cudaLaunchKernelEx(&cfg, k_sor32p<0, false>, d, c->g, r, e, o, c->packed_lp, omega, om1);
     else cudaLaunchKernelEx(&cfg, k_sor32p<1, false>, d, c->g, r, e, o, c->packed_lp, omega, om1);
   }
+}
+
+// Where the four packed arrays fit in L2 with room to spare, one colour pass per
+// launch of the two-row kernel; beyond 96 MB the one-row kernel with branch-free
+// loads, which keeps more DRAM requests in flight (at 384x256x256: 79.9 us per sweep
+// against 82.5 for the two-row kernel).
+static bool two_row_kernel(const ib3d_ctx* c) {
+  const Dims& d = c->d;
+  const size_t packed = 4 * sizeof(float) * (size_t)c->packed_lp * (size_t)d.NY2 * (size_t)d.NZ2;
+  return c->prm.sweep_kernel == 0 && packed <= ((size_t)96 << 20);
+}
+
+// One colour pass of the two-row kernel.
+static void launch_pass2(ib3d_ctx* c, int color, float omega, float om1) {
+  const Dims& d = c->d;
+  const int nq = ((d.nx >> 1) + 3) >> 2;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((nq + 31) / 32), (unsigned)((d.ny + 2 * kRows2 - 1) / (2 * kRows2)),
+                     (unsigned)((d.nz + kPlanes2 - 1) / kPlanes2));
+  cfg.blockDim = dim3(32, kRows2);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const float* r = c->rp[color];
+  float* e = c->ep[color];
+  const float* o = c->ep[1 - color];
+  if (color == 0) cudaLaunchKernelEx(&cfg, k_sor32p2<0>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+  else cudaLaunchKernelEx(&cfg, k_sor32p2<1>, d, c->g, r, e, o, c->packed_lp, omega, om1);
+}
+
+// One red-black sweep with the colour-packed two-pass kernels.
+void launch_sor32_sweep(ib3d_ctx* c, float omega, float om1) {
+  if (two_row_kernel(c)) {
+    launch_pass2(c, 0, omega, om1);
+    launch_pass2(c, 1, omega, om1);
+  } else {
+    launch_sor32_packed(c, 0, omega, om1);
+    launch_sor32_packed(c, 1, omega, om1);
+  }
+}
+
+// Sweeps per replay of the captured sweep graph: the host issues one graph launch
+// per kGraphSweeps sweeps instead of two kernel launches per sweep (a pass takes
+// about 8 us), so the sweep loop does not depend on the host's launch rate.
+constexpr int kGraphSweeps = 32;
+
+// Captures kGraphSweeps sweeps at (omega, om1) as a CUDA graph on the context's
+// stream, unless the cached one was captured with the same tables, relaxation and
+// kernel choice. Returns false when capture or instantiation fails (the caller then
+// launches the sweeps one by one).
+static bool ensure_sweep_graph(ib3d_ctx* c, float omega, float om1) {
+  if (c->sweep_exec && c->sweep_w == omega && c->sweep_w1 == om1 && c->sweep_kern == c->prm.sweep_kernel &&
+      std::memcmp(&c->sweep_g, &c->g, sizeof(Grid1D)) == 0)
+    return true;
+  if (c->sweep_exec) {
+    cudaGraphExecDestroy(c->sweep_exec);
+    c->sweep_exec = nullptr;
+  }
+  if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  for (int q = 0; q < kGraphSweeps; ++q) launch_sor32_sweep(c, omega, om1);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+  bool ok = e == cudaSuccess && graph != nullptr &&
+            cudaGraphInstantiate(&c->sweep_exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok) {
+    c->sweep_exec = nullptr;
+    cudaGetLastError();
+    return false;
+  }
+  c->sweep_w = omega;
+  c->sweep_w1 = om1;
+  c->sweep_kern = c->prm.sweep_kernel;
+  c->sweep_g = c->g;
+  return true;
+}
+
+// n red-black sweeps at (omega, om1) with the colour-packed kernels: whole groups of
+// kGraphSweeps as replays of the captured graph, the rest launched directly.
+void run_sor32_sweeps(ib3d_ctx* c, int n, float omega, float om1) {
+  if (n >= kGraphSweeps && !c->sweep_graph_failed) {
+    if (ensure_sweep_graph(c, omega, om1)) {
+      for (; n >= kGraphSweeps; n -= kGraphSweeps) cudaGraphLaunch(c->sweep_exec, c->st);
+    } else {
+      c->sweep_graph_failed = true;
+    }
+  }
+  for (; n > 0; --n) launch_sor32_sweep(c, omega, om1);
 }
 
 // Rows per block and stages of the staged sweep for a row of nq float4 groups: 16 rows

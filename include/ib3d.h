@@ -81,11 +81,12 @@ typedef struct ib3d_params {
   int32_t warm_start;   /* IB3D_WARM_* */
   int32_t check_every;  /* sweeps between residual checks (IB3D_CRIT_RESIDUAL); >= 1 */
   int32_t inner_sweeps; /* FP32 sweeps per defect-correction pass (IB3D_PREC_FP32DC) */
-  int32_t sweep_kernel; /* FP32 sweep kernel: 0 colour-packed arrays, one launch per colour pass (even
-                           nx; its loads run without branches when the arrays exceed L2); 1 the
-                           padded field layout; 2 colour-packed arrays, the red and black passes
-                           fused into one z-wavefront launch per sweep (even nx <= 512); 3 as 0 with
-                           the branch-free loads at every size. All give the same results. */
+  int32_t sweep_kernel; /* FP32 sweep kernel: 0 colour-packed arrays (even nx), one launch per colour
+                           pass, two rows per thread (as 3 where the packed arrays exceed L2);
+                           1 the padded field layout; 2 colour-packed arrays, the red and black
+                           passes fused into one z-wavefront launch per sweep (even nx <= 512); 3
+                           and 4 colour-packed arrays, one row per thread, the loads without (3)
+                           or behind (4) branches. All give the same results. */
   double omega_inner;   /* relaxation factor of the FP32 inner sweeps (0: use omega). The FP64
                            defect correction fixes the final accuracy, so the inner solve may use
                            its own factor. */

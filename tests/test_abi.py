@@ -39,7 +39,7 @@ def test_python_mirror_binds_every_symbol(ib3d, built_lib):
 
 def test_params_struct_layout(ib3d, built_lib):
     p = ib3d.default_params()
-    # 4 doubles, int64, 6 int32, double, 3 int32 + 4 bytes of tail padding
+    # 4 doubles, int64, 6 int32, double, 5 int32 + 4 bytes of tail padding
     assert ctypes.sizeof(ib3d.Params) == 8 * 4 + 8 + 4 * 6 + 8 + 5 * 4 + 4   # padded to 8 bytes
     assert ib3d.Params.omega_inner.offset == 64 and ib3d.Params.inner_schedule.offset == 72
     assert ib3d.Params.outlet.offset == 76 and ib3d.Params.momentum.offset == 80

@@ -200,17 +200,20 @@ def test_mixed_precision_matches_fp64_drag(ib3d, grids):
     s64.close(); s32.close()
 
 
-@pytest.mark.parametrize("name,kernel", [("tiny", 0), ("small", 0), ("tiny", 2), ("small", 2), ("small", 3)])
-def test_packed_fp32_sweep_matches_padded_layout(ib3d, grids, name, kernel):
-    """The FP32 sweep on colour-packed arrays (two colour passes, kernel 0; the same with
-    its loads free of branches, kernel 3; or one fused z-wavefront launch per sweep,
-    kernel 2) performs the same red-then-black
-    update with the same FP32 operation order as the sweep on the padded field
-    layout, so whole mixed-precision steps agree bit for bit."""
+@pytest.mark.parametrize("name,kernel,inner", [("tiny", 0, 7), ("small", 0, 7), ("small", 0, 40), ("tiny", 2, 7),
+                                               ("small", 2, 7), ("small", 3, 7), ("small", 3, 40), ("tiny", 4, 7),
+                                               ("small", 4, 7)])
+def test_packed_fp32_sweep_matches_padded_layout(ib3d, grids, name, kernel, inner):
+    """The FP32 sweep on colour-packed arrays (two colour passes with two rows per
+    thread, kernel 0; with one row per thread and the loads free of branches, kernel 3,
+    or behind branches, kernel 4; or one fused z-wavefront launch per sweep, kernel 2)
+    performs the same red-then-black update with the same FP32 operation order as the
+    sweep on the padded field layout, so whole mixed-precision steps agree bit for bit.
+    Passes of 40 sweeps run 32 of them as one replay of the captured sweep graph."""
     cs = grids.case(name)
     common = dict(precision=ib3d.PREC_FP32DC, criterion=ib3d.CRIT_RESIDUAL, eps=1e-6, inner_sweeps=7)
-    a = ib3d.setup_case(cs, sweep_kernel=kernel, **common)
-    b = ib3d.setup_case(cs, sweep_kernel=1, **common)
+    a = ib3d.setup_case(cs, sweep_kernel=kernel, **dict(common, inner_sweeps=inner))
+    b = ib3d.setup_case(cs, sweep_kernel=1, **dict(common, inner_sweeps=inner))
     for step in range(1, 4):
         sa, ca = a.step(step == 1)
         sb, cb = b.step(step == 1)

@@ -77,8 +77,10 @@ def test_neumann_cube_fp32_sweeps_reach_fp64_residual(ib3d, grids):
 
 @pytest.mark.parametrize("shape", [(300, 20, 18), (258, 17, 9), (64, 33, 31)])
 def test_packed_sweep_on_ragged_rows_matches_padded_layout(ib3d, grids, shape):
-    """The colour-packed FP32 sweeps (two colour passes with and without branches
-    around the loads, and the fused z-wavefront sweep) against the one-array sweep on rows whose float4 groups fill no whole
+    """The colour-packed FP32 sweeps (two colour passes with two rows per thread, or
+    with one row per thread with and without branches around the loads, each pass of
+    64 sweeps as two replays of the captured 32-sweep graph; and the fused z-wavefront
+    sweep) against the one-array sweep on rows whose float4 groups fill no whole
     warp or spill into a second one (nx = 300: 38 groups; 258: 33; 64: 8), odd ny
     and nz, and row and plane counts that are no multiple of a block's rows or
     planes: all perform the same FP32 operations, so the sweep counts and the
@@ -88,7 +90,8 @@ def test_packed_sweep_on_ragged_rows_matches_padded_layout(ib3d, grids, shape):
     b = grids.divergence_rhs(x, y, z, grids.random_face_velocities(shape, 3))
     acoef = (grids.neumann_coefficients(x), grids.neumann_coefficients(y), grids.neumann_coefficients(z))
     out = []
-    for kernel in (1, 0, 2, 3):
+    configs = (1, 0, 2, 3, 4)   # sweep_kernel
+    for kernel in configs:
         p = ib3d.default_params(re=100.0, deltat=1.0, omega=1.85, eps=1e-8, max_sweeps=200000)
         p.precision, p.criterion, p.inner_sweeps, p.sweep_kernel = ib3d.PREC_FP32DC, 1, 64, kernel
         s = ib3d.Solver(x, y, z, p)
@@ -98,7 +101,7 @@ def test_packed_sweep_on_ragged_rows_matches_padded_layout(ib3d, grids, shape):
         assert st["final_err"] < 1e-8
         out.append((st["sweeps"], s.get_field("pc")))
         s.close()
-    for q in (1, 2, 3):
-        assert out[q][0] == out[0][0], (q, out[q][0], out[0][0])
+    for q in range(1, len(configs)):
+        assert out[q][0] == out[0][0], (configs[q], out[q][0], out[0][0])
         bad = np.argwhere(out[q][1] != out[0][1])
-        assert bad.size == 0, f"kernel {(1, 0, 2, 3)[q]}: {len(bad)} pc mismatches, first {bad[0]}"
+        assert bad.size == 0, f"kernel {configs[q]}: {len(bad)} pc mismatches, first {bad[0]}"
