@@ -59,12 +59,13 @@ HEADLINE_RE = 275.0
 # written 4 + r 4 + flag 1; FP64 sweep = pc read 8 + written 8 + b/dt 8 + flag 1.
 BYTES_SOR32_SWEEP = 13.0
 BYTES_SOR64_SWEEP = 25.0
-# DRAM bytes (read + written) per grid cell and sweep of the FP32 sweep kernel at
-# 256x192x192, from one ncu capture of the launches inside the sweep loop (warm: caches as
-# the previous launch left them) and of a launch after a cache flush (cold). Other
-# workloads scale them by their cell count.
-DRAM_BYTES_PER_CELL_SWEEP32 = 2 * 22946560.0 / 4 / 9437184.0
-DRAM_BYTES_PER_CELL_SWEEP32_COLD = 2 * 60741760.0 / 9437184.0
+# DRAM bytes (read + written) per grid cell and sweep of the FP32 sweep kernel
+# (k_sor32p2) at 256x192x192, from one ncu capture of four launches inside the sweep
+# loop (warm: caches as the previous launch left them; 9,702,144 B in all) and of two
+# launches after a cache flush (cold; 60,701,696 B each on average). Other workloads
+# scale them by their cell count.
+DRAM_BYTES_PER_CELL_SWEEP32 = 2 * 9702144.0 / 4 / 9437184.0
+DRAM_BYTES_PER_CELL_SWEEP32_COLD = 2 * 60701696.0 / 9437184.0
 
 
 def package():
