@@ -213,27 +213,31 @@ __global__ void __launch_bounds__(32 * kRows2, 4) k_sor32p2(Dims d, Grid1D g, co
                                                                     float* __restrict__ e_own,
                                                                     const float* __restrict__ e_oth, int Lp, float omega,
                                                                     float om1) {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nq = ((d.nx >> 1) + 3) >> 2;
   const int lane = threadIdx.x;
   const int q = blockIdx.x * 32 + lane;
   const int ja = blockIdx.y * (2 * kRows2) + 2 * threadIdx.y + 2;
   const int k0 = blockIdx.z * kPlanes2 + 2;
-  if (ja <= d.ny + 1) {   // uniform across the warp, so the shuffles see all lanes
-    const bool lds = q < nq;
-    const bool rowb = ja + 1 <= d.ny + 1;
+  const bool live = ja <= d.ny + 1;   // uniform across the warp, so the shuffles see all lanes
+  const bool lds = live && q < nq;
+  const bool rowb = ja + 1 <= d.ny + 1;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  // the coefficient tables are written by the host before the solve, never by a
+  // kernel, so they load before the wait for the previous pass
+  const float ya0 = live ? g.acy32[0][ja - 1] : 0.f, ya1 = live ? g.acy32[1][ja - 1] : 0.f,
+              ya2 = live ? g.acy32[2][ja - 1] : 0.f;
+  const float yb0 = rowb ? g.acy32[0][ja] : 0.f, yb1 = rowb ? g.acy32[1][ja] : 0.f,
+              yb2 = rowb ? g.acy32[2][ja] : 0.f;
+  // P: the phase of row a at even planes (and of row b at odd ones); Q the other
+  const float4 p0 = lds ? g.axp[1 - COLOR][0][q] : z4, p1 = lds ? g.axp[1 - COLOR][1][q] : z4,
+               p2 = lds ? g.axp[1 - COLOR][2][q] : z4;
+  const float4 q0 = lds ? g.axp[COLOR][0][q] : z4, q1 = lds ? g.axp[COLOR][1][q] : z4,
+               q2 = lds ? g.axp[COLOR][2][q] : z4;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (live) {
     const bool load_left = lane == 0, load_right = lane == 31 || q + 1 >= nq;
     const int plane = (d.ny + 2) * Lp;
     const int sa = (ja - 1) * Lp + 4 * q + 4;
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float ya0 = g.acy32[0][ja - 1], ya1 = g.acy32[1][ja - 1], ya2 = g.acy32[2][ja - 1];
-    const float yb0 = rowb ? g.acy32[0][ja] : 0.f, yb1 = rowb ? g.acy32[1][ja] : 0.f,
-                yb2 = rowb ? g.acy32[2][ja] : 0.f;
-    // P: the phase of row a at even planes (and of row b at odd ones); Q the other
-    const float4 p0 = lds ? g.axp[1 - COLOR][0][q] : z4, p1 = lds ? g.axp[1 - COLOR][1][q] : z4,
-                 p2 = lds ? g.axp[1 - COLOR][2][q] : z4;
-    const float4 q0 = lds ? g.axp[COLOR][0][q] : z4, q1 = lds ? g.axp[COLOR][1][q] : z4,
-                 q2 = lds ? g.axp[COLOR][2][q] : z4;
     float4 oba = lds ? ld4(e_oth + (k0 - 2) * plane + sa) : z4, obb = lds ? ld4(e_oth + (k0 - 2) * plane + sa + Lp) : z4;
     float4 oxa = lds ? ld4(e_oth + (k0 - 1) * plane + sa) : z4, oxb = lds ? ld4(e_oth + (k0 - 1) * plane + sa + Lp) : z4;
 #pragma unroll
@@ -613,12 +617,14 @@ void launch_sor32_packed(ib3d_ctx* c, int color, float omega, float om1) {
 
 // Where the four packed arrays fit in L2 with room to spare, one colour pass per
 // launch of the two-row kernel; beyond 96 MB the one-row kernel with branch-free
-// loads, which keeps more DRAM requests in flight (at 384x256x256: 79.9 us per sweep
-// against 82.5 for the two-row kernel).
+// loads, which keeps more DRAM requests in flight (at 384x256x256, 213 MB: 79.7 us
+// per sweep against 82.5-85.2 for the two-row kernel; at 256^3, 145 MB, the two are
+// within 2 %).
+constexpr size_t kTwoRowMaxBytes = (size_t)96 << 20;
 static bool two_row_kernel(const ib3d_ctx* c) {
   const Dims& d = c->d;
   const size_t packed = 4 * sizeof(float) * (size_t)c->packed_lp * (size_t)d.NY2 * (size_t)d.NZ2;
-  return c->prm.sweep_kernel == 0 && packed <= ((size_t)96 << 20);
+  return c->prm.sweep_kernel == 0 && packed <= kTwoRowMaxBytes;
 }
 
 // One colour pass of the two-row kernel.
