@@ -361,8 +361,14 @@ def coef_errors(coefs, ref_coefs) -> dict:
     return {"drag_rel": cd_err, "lift_rel": cl_err, "steps_compared": min(len(coefs), len(ref_coefs))}
 
 
-def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None, restart: str | None = None):
-    """The headline form through the C ABI with pinned host buffers in the timed region."""
+def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None, restart: str | None = None,
+            overlap: bool = True):
+    """The headline form through the C ABI with pinned host buffers in the timed region:
+    the inputs uploaded once, then every step followed by the download of its seven
+    fields, and the clock stops when the last download has landed. overlap: the
+    download is ib3d_download_fields_async (a device snapshot, then host copies that
+    run during the next step; a final ib3d_download_wait), else the blocking
+    ib3d_download_fields."""
     import torch
     s = pkg.setup_case(cs, **mode)
     if net is not None:
@@ -391,7 +397,11 @@ def run_e2e(pkg, cs, mode: dict, warmup: int, steps: int, dist: Dist, net=None, 
     for _ in range(steps):
         s.step(first)
         first = False
-        s.download_fields(host_out)
+        if overlap:
+            s.download_fields_async(host_out)
+        else:
+            s.download_fields(host_out)
+    s.download_wait()
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
@@ -984,8 +994,10 @@ def main():
     if "e2e" in arms:
         e2e = run_e2e(pkg, cs, head_mode, warmup, args.steps, dist, net=net)
         e2e_value = dist.world * args.steps / dist.max(e2e["seconds"])
+        blocking = run_e2e(pkg, cs, head_mode, warmup, args.steps, dist, net=net, overlap=False)
+        e2e["blocking_value"] = dist.world * args.steps / dist.max(blocking["seconds"])
     else:
-        e2e, e2e_value = {"h2d": None, "d2h": None}, None
+        e2e, e2e_value = {"h2d": None, "d2h": None, "blocking_value": None}, None
 
     errs = coef_errors(head["coefs"], ref_run["coefs"]) if ref_run is not None else None
     line = {
@@ -1027,7 +1039,10 @@ def main():
                      "share_of_step": tm["sor32_ms"] / phase_total if phase_total else None,
                      "peak_source": peak_src},
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": e2e["h2d"],
-                "d2h_bytes_per_step": e2e["d2h"]},
+                "d2h_bytes_per_step": e2e["d2h"],
+                "download": "ib3d_download_fields_async every step (device snapshot of the seven fields, host "
+                            "copies overlapped with the next step), ib3d_download_wait before the clock stops",
+                "blocking_download_value": e2e["blocking_value"]},
         "gpu_launches": tm["launches"],
         "clocks": head["clocks"],
     }

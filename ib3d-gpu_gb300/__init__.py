@@ -123,6 +123,8 @@ def lib() -> C.CDLL:
         "ib3d_initial_conditions": (C.c_int, [_VP]),
         "ib3d_upload_fields": (C.c_int, [_VP, _D, _D, _D, _D]),
         "ib3d_download_fields": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _D]),
+        "ib3d_download_fields_async": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _D]),
+        "ib3d_download_wait": (C.c_int, [_VP]),
         "ib3d_get_field": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_set_field": (C.c_int, [_VP, C.c_int, _D]),
         "ib3d_ns_momentum": (C.c_int, [_VP]),
@@ -325,6 +327,17 @@ class Solver:
         out = out if out is not None else {n: np.empty(self.shape, dtype=np.float64, order="F") for n in names}
         self._check(self.L.ib3d_download_fields(self._h, *(_dp(out[n]) for n in names)), "ib3d_download_fields")
         return out
+
+    def download_fields_async(self, out: dict) -> dict:
+        """Starts the download of the seven fields into `out` (arrays that stay alive and
+        unread until download_wait); returns at once."""
+        names = ("u", "v", "w", "ut", "vt", "wt", "p")
+        self._check(self.L.ib3d_download_fields_async(self._h, *(_dp(out[n]) for n in names)),
+                    "ib3d_download_fields_async")
+        return out
+
+    def download_wait(self):
+        self._check(self.L.ib3d_download_wait(self._h), "ib3d_download_wait")
 
     def device_field(self, name: str) -> int:
         return self.L.ib3d_device_field(self._h, FIELDS[name]) or 0

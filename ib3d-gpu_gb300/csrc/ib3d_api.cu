@@ -513,8 +513,15 @@ void ib3d_destroy(ib3d_ctx* c) {
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (cudaStream_t x : c->xfer)
-    if (x) cudaStreamDestroy(x);
+    if (x) {
+      cudaStreamSynchronize(x);
+      cudaStreamDestroy(x);
+    }
+  if (c->stage) cudaFree(c->stage);
   if (c->xfer_ready) cudaEventDestroy(c->xfer_ready);
+  if (c->staged) cudaEventDestroy(c->staged);
+  for (cudaEvent_t e : c->xfer_done)
+    if (e) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -696,6 +703,16 @@ int ib3d_upload_fields(ib3d_ctx* c, const double* u, const double* v, const doub
   return IB3D_OK;
 }
 
+// The transfer streams of the host downloads and their events, created on first use.
+static int ensure_xfer(ib3d_ctx* c) {
+  if (c->xfer_ready) return IB3D_OK;
+  IB3D_CUDA(c, cudaEventCreateWithFlags(&c->xfer_ready, cudaEventDisableTiming));
+  IB3D_CUDA(c, cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming));
+  for (auto& e : c->xfer_done) IB3D_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  return IB3D_OK;
+}
+
 int ib3d_download_fields(ib3d_ctx* c, double* u, double* v, double* w, double* ut, double* vt, double* wt,
                          double* p) {
   if (!c) return IB3D_ERR_ARG;
@@ -705,10 +722,8 @@ int ib3d_download_fields(ib3d_ctx* c, double* u, double* v, double* w, double* u
   // the copies go round-robin over the context's stream and three more, which start
   // once the work queued on the context's stream is done, so that several copy engines
   // share the host link; the call returns when all of them have landed
-  if (!c->xfer_ready) {
-    IB3D_CUDA(c, cudaEventCreateWithFlags(&c->xfer_ready, cudaEventDisableTiming));
-    for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
-  }
+  int rc = ensure_xfer(c);
+  if (rc) return rc;
   IB3D_CUDA(c, cudaEventRecord(c->xfer_ready, c->st));
   for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamWaitEvent(x, c->xfer_ready, 0));
   int n = 0;
@@ -720,6 +735,46 @@ int ib3d_download_fields(ib3d_ctx* c, double* u, double* v, double* w, double* u
     }
   IB3D_CUDA(c, cudaStreamSynchronize(c->st));
   for (auto& x : c->xfer) IB3D_CUDA(c, cudaStreamSynchronize(x));
+  c->async_pending = false;
+  return IB3D_OK;
+}
+
+int ib3d_download_fields_async(ib3d_ctx* c, double* u, double* v, double* w, double* ut, double* vt, double* wt,
+                               double* p) {
+  if (!c) return IB3D_ERR_ARG;
+  const size_t n3 = (size_t)c->d.n3, bytes = n3 * sizeof(double);
+  double* dst[7] = {u, v, w, ut, vt, wt, p};
+  const double* src[7] = {c->u, c->v, c->w, c->ut, c->vt, c->wt, c->p};
+  int rc = ensure_xfer(c);
+  if (rc) return rc;
+  if (!c->stage && cudaMalloc(&c->stage, 7 * bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, IB3D_ERR_MEMORY, "ib3d_download_fields_async: no device memory for the snapshot");
+  }
+  // the snapshot may be overwritten only once the previous call's host copies have read it
+  if (c->async_pending)
+    for (auto& e : c->xfer_done) IB3D_CUDA(c, cudaStreamWaitEvent(c->st, e, 0));
+  for (int q = 0; q < 7; ++q)
+    if (dst[q]) IB3D_CUDA(c, cudaMemcpyAsync(c->stage + q * n3, src[q], bytes, cudaMemcpyDeviceToDevice, c->st));
+  IB3D_CUDA(c, cudaEventRecord(c->staged, c->st));
+  int n = 0;
+  for (int q = 0; q < 7; ++q)
+    if (dst[q]) {
+      cudaStream_t x = c->xfer[n % 3];
+      if (n < 3) IB3D_CUDA(c, cudaStreamWaitEvent(x, c->staged, 0));
+      IB3D_CUDA(c, cudaMemcpyAsync(dst[q], c->stage + q * n3, bytes, cudaMemcpyDeviceToHost, x));
+      ++n;
+    }
+  for (int i = 0; i < 3; ++i) IB3D_CUDA(c, cudaEventRecord(c->xfer_done[i], c->xfer[i]));
+  c->async_pending = true;
+  return IB3D_OK;
+}
+
+int ib3d_download_wait(ib3d_ctx* c) {
+  if (!c) return IB3D_ERR_ARG;
+  if (!c->async_pending) return IB3D_OK;
+  for (auto& e : c->xfer_done) IB3D_CUDA(c, cudaEventSynchronize(e));
+  c->async_pending = false;
   return IB3D_OK;
 }
 
@@ -895,7 +950,9 @@ int ib3d_poisson_solver(ib3d_ctx* c, ib3d_solve_stats* stats) {
     cudaEventElapsedTime(&ms, e0, e1);
     st.solve_seconds = ms * 1e-3;
     std::memcpy(&st.divmax, &h[0], sizeof(double));
-    std::memcpy(&st.derr_std_st, &h[1], sizeof(double));
+    double dmax = 0.0;   // max |ut-u| over the fluid cells (k_dss_copy)
+    std::memcpy(&dmax, &h[1], sizeof(double));
+    st.derr_std_st = dmax / c->prm.deltat;
     if (c->prm.warm_start == IB3D_WARM_LEARNED) net_note_failure(c);
   }
   cudaEventDestroy(e0);

@@ -115,6 +115,13 @@ struct ib3d_ctx {
   // use), and the event that orders them after the work on st
   cudaStream_t xfer[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t xfer_ready = nullptr;
+  // ib3d_download_fields_async: device snapshot of the seven fields (allocated on first
+  // use), the event after the snapshot, one event per transfer stream after its host
+  // copies, and whether such copies may still be in flight
+  double* stage = nullptr;
+  cudaEvent_t staged = nullptr;
+  cudaEvent_t xfer_done[3] = {nullptr, nullptr, nullptr};
+  bool async_pending = false;
   int device = 0;
   std::string err;
 

@@ -304,10 +304,14 @@ __global__ void k_solid_bc(Dims d, const unsigned char* __restrict__ cell, doubl
 }
 
 // Steady-state indicator derrStdSt = max |ut-u|/dt (subPcorVcor.f90:45-58) over fluid
-// cells, fused with the copy u = ut, v = vt, w = wt of the whole array (:67-77).
+// cells, fused with the copy u = ut, v = vt, w = wt of the whole array (:67-77). The
+// kernel reduces max |ut-u| and the caller divides the maximum by dt once: rounded
+// division by a positive number is monotone, so the quotient of the maximum is the
+// maximum of the per-cell quotients, bit for bit, without three FP64 divisions per
+// cell.
 __global__ void k_dss_copy(Dims d, const unsigned char* __restrict__ cell, double* __restrict__ u,
                            double* __restrict__ v, double* __restrict__ w, const double* __restrict__ ut,
-                           const double* __restrict__ vt, const double* __restrict__ wt, double deltat,
+                           const double* __restrict__ vt, const double* __restrict__ wt,
                            unsigned long long* acc) {
   const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
   double m = 0.0;
@@ -316,9 +320,9 @@ __global__ void k_dss_copy(Dims d, const unsigned char* __restrict__ cell, doubl
     int i, j, k;
     decode(d, idx, i, j, k);
     if (interior(d, i, j, k) && cell[idx] == 0) {
-      const double du = fabs(a - u[idx]) / deltat;
-      const double dv = fabs(bb - v[idx]) / deltat;
-      const double dw = fabs(c - w[idx]) / deltat;
+      const double du = fabs(a - u[idx]);
+      const double dv = fabs(bb - v[idx]);
+      const double dw = fabs(c - w[idx]);
       m = nan_max(nan_max(du, dv), dw);
     }
     u[idx] = a; v[idx] = bb; w[idx] = c;
@@ -390,7 +394,7 @@ void launch_dss_copy(ib3d_ctx* c) {
   PhaseScope ps(c, PH_CORRECT);
   c->launches += 1;
   k_dss_copy<<<nblocks(c->d.n3), kBlock, 0, c->st>>>(c->d, c->cell, c->u, c->v, c->w, c->ut, c->vt, c->wt,
-                                                      c->prm.deltat, &c->ctl->aux);
+                                                      &c->ctl->aux);
 }
 
 void launch_initial(ib3d_ctx* c) {

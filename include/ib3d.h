@@ -221,6 +221,17 @@ int ib3d_upload_fields(ib3d_ctx* ctx, const double* u, const double* v, const do
 /* `!$acc update host (u, v, w, ut, vt, wt, p, cell)` (main.f90:55). Any pointer may be NULL. */
 int ib3d_download_fields(ib3d_ctx* ctx, double* u, double* v, double* w, double* ut, double* vt,
                          double* wt, double* p);
+/* The same download without waiting for it (the host side of main.f90:55 overlapped with the next
+ * step): the fields as they stand after the work queued so far are copied to a device snapshot on
+ * the context's stream (544 MB at 256x192x192, allocated on the first call), and the host copies
+ * run from the snapshot on separate streams while the caller queues the next step. The host
+ * buffers must stay valid, and unread, until ib3d_download_wait returns; pinned host memory lets
+ * the copies run asynchronously. A second call first waits, on the device, for the previous
+ * call's copies to leave the snapshot. */
+int ib3d_download_fields_async(ib3d_ctx* ctx, double* u, double* v, double* w, double* ut, double* vt,
+                               double* wt, double* p);
+/* Blocks until the host copies of the last ib3d_download_fields_async have landed. */
+int ib3d_download_wait(ib3d_ctx* ctx);
 /* Read back one device field: 0 u,1 v,2 w,3 ut,4 vt,5 wt,6 p,7 pc,8 b. */
 int ib3d_get_field(ib3d_ctx* ctx, int which, double* out);
 /* Write one device field (same numbering); for tests that start a routine from a given state. */

@@ -248,6 +248,36 @@ def test_download_matches_get_field(ib3d, grids):
     s.close()
 
 
+def test_async_download_holds_the_fields_of_its_step(ib3d, grids):
+    """ib3d_download_fields_async snapshots the fields on the device, so the host
+    buffers receive the fields of the step it was called after even while the next
+    steps run and change them; two calls in a row keep their order."""
+    import torch
+    cs = grids.case("small")
+    s = ib3d.setup_case(cs, precision=ib3d.PREC_FP32DC, criterion=ib3d.CRIT_RESIDUAL, eps=1e-6)
+    names = ("u", "v", "w", "ut", "vt", "wt", "p")
+    n3 = s.shape[0] * s.shape[1] * s.shape[2]
+
+    def pinned():
+        return torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy().reshape(s.shape, order="F")
+
+    a, b = {f: pinned() for f in names}, {f: pinned() for f in names}
+    s.step(True)
+    ref1 = s.download_fields()
+    s.download_fields_async(a)
+    s.step(False)
+    ref2 = s.download_fields()
+    s.download_fields_async(b)
+    s.step(False)
+    s.step(False)
+    s.download_wait()
+    for f in names:
+        _same(a[f], ref1[f], f)
+        _same(b[f], ref2[f], f)
+    assert not np.array_equal(ref1["u"], ref2["u"])
+    s.close()
+
+
 @pytest.mark.parametrize("outlet,momentum", [(1, 0), (0, 1), (1, 1)])
 def test_convective_outlet_and_ab2_steps_bit_exact(ib3d, oracle_mod, grids, outlet, momentum):
     """The reference's optional branches: Orlanski outlet with calculateUc after each
