@@ -308,6 +308,9 @@ static void poisson32_host(const ib3d_ctx* c, std::vector<float>& h32, std::vect
               hp[(((size_t)s * 3 + q) * nq + g) * 4 + e] = q == 1 ? a : -a;
             }
           }
+    // then the three z coefficients of each plane as one float4 (Grid1D::acz4)
+    for (size_t m = 0; m < c->hac[2][0].size(); ++m)
+      for (int q = 0; q < 4; ++q) hp.push_back(q < 3 ? (float)c->hac[2][q][m] : 0.0f);
   }
 }
 
@@ -470,6 +473,7 @@ int ib3d_create(ib3d_ctx** out, const ib3d_params* prm, int64_t nx, int64_t ny, 
         for (int s = 0; s < 2; ++s)
           for (int q = 0; q < 3; ++q)
             c->g.axp[s][q] = reinterpret_cast<const float4*>(c->d_axp) + ((size_t)s * 3 + q) * nq;
+        c->g.acz4 = reinterpret_cast<const float4*>(c->d_axp) + (size_t)6 * nq;
       }
       rc = upload_poisson32(c, h32, hp);
     }

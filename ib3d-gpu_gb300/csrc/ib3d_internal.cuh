@@ -47,6 +47,8 @@ struct Grid1D {
   // starts at i = 2, s = 1 at i = 3), as FP32 float4; columns c = 0 and 2 (the
   // off-diagonal ones) are stored negated
   const float4* axp[2][3];
+  // acz32[0..2][m] as one float4 per plane (w = 0), for the colour-packed sweep
+  const float4* acz4;
   // convection tables cc[fam][m], fam 0 uu,1 vv,2 ww,3 uv(=uw),4 vu(=vw),5 wu(=wv)
   const double* cc[6][12];
   // velocity-correction factor deltat/(0.5*(d(i+1)+d(i))) per axis

@@ -268,7 +268,8 @@ __global__ void __launch_bounds__(32 * kRows2, 4) k_sor32p2(Dims d, Grid1D g, co
         ra_ = e_oth[s0 + 4];
         rb_ = e_oth[s0 + Lp + 4];
       }
-      const float z0 = g.acz32[0][k - 1], z1 = g.acz32[1][k - 1], z2 = g.acz32[2][k - 1];
+      const float4 zc = g.acz4[k - 1];
+      const float z0 = zc.x, z1 = zc.y, z2 = zc.z;
       if (lds) {
         const float xa[6] = {la, oxa.x, oxa.y, oxa.z, oxa.w, ra_};
         const float xb[6] = {lb, oxb.x, oxb.y, oxb.z, oxb.w, rb_};
