@@ -8,7 +8,7 @@ the headline form (FP32 red-black sweeps inside FP64 defect correction, the benc
 pass schedule, Gauss-Seidel smoothing and relaxation ramp, learned warm start with
 the default network) run the same 8 steps. At every step both solves must end below
 the residual tolerance, and the drag and lift of the headline form must lie within
-1e-4 relative of the plain path's (the benchmark spec's bar for the mixed-precision and
+1e-4 relative of the plain path's (the required bar for the mixed-precision and
 learned forms). After the last step u, v, w and p must agree within 1e-7 of each
 field's largest magnitude (measured: ~1e-9 after 20 steps).
 
@@ -74,7 +74,7 @@ def test_headline_form_matches_plain_fp64_at_the_bench_configuration(ib3d):
 def test_fast_plain_fp64_matches_the_reference_arithmetic_at_the_bench_configuration(ib3d):
     """The fast plain FP64 form (contracted multiply-adds, omega/diag per cell) over
     4 steps of the same workload: drag within 1e-6 and fields within 1e-8 of the
-    bit-identical path (the benchmark spec's bar for the plain path)."""
+    bit-identical path (the required bar for the plain path)."""
     bench = _bench()
     cs = bench.workload(ib3d, "sphere256", bench.HEADLINE_RE)
     a = ib3d.setup_case(cs, **bench.PLAIN)

@@ -90,8 +90,8 @@ def test_packed_sweep_on_ragged_rows_matches_padded_layout(ib3d, grids, shape):
     b = grids.divergence_rhs(x, y, z, grids.random_face_velocities(shape, 3))
     acoef = (grids.neumann_coefficients(x), grids.neumann_coefficients(y), grids.neumann_coefficients(z))
     out = []
-    configs = (1, 0, 2, 3, 4)   # sweep_kernel
-    for kernel in configs:
+    kernels = (1, 0, 2, 3, 4)   # sweep_kernel
+    for kernel in kernels:
         p = ib3d.default_params(re=100.0, deltat=1.0, omega=1.85, eps=1e-8, max_sweeps=200000)
         p.precision, p.criterion, p.inner_sweeps, p.sweep_kernel = ib3d.PREC_FP32DC, 1, 64, kernel
         s = ib3d.Solver(x, y, z, p)
@@ -101,7 +101,7 @@ def test_packed_sweep_on_ragged_rows_matches_padded_layout(ib3d, grids, shape):
         assert st["final_err"] < 1e-8
         out.append((st["sweeps"], s.get_field("pc")))
         s.close()
-    for q in range(1, len(configs)):
-        assert out[q][0] == out[0][0], (configs[q], out[q][0], out[0][0])
+    for q in range(1, len(kernels)):
+        assert out[q][0] == out[0][0], (kernels[q], out[q][0], out[0][0])
         bad = np.argwhere(out[q][1] != out[0][1])
-        assert bad.size == 0, f"kernel {configs[q]}: {len(bad)} pc mismatches, first {bad[0]}"
+        assert bad.size == 0, f"kernel {kernels[q]}: {len(bad)} pc mismatches, first {bad[0]}"
