@@ -98,3 +98,13 @@ def test_noalloc_rejects_extents_beyond_its_scratch_before_any_cuda_call(ib3d):
         rc = L.ib3d_pressure_solve_noalloc(*n, dummy, dummy, dummy, dummy, dummy, 0.001, dummy, 1.9, 1e-6, 10, 4,
                                            None, None, None)
         assert rc == ib3d.ERR_TOO_LARGE, (n, rc)
+
+
+def test_download_entry_points_reject_a_null_context(ib3d, built_lib):
+    """The blocking and the asynchronous download and its wait check their context
+    before touching the device: a null context is IB3D_ERR_ARG, with no CUDA call."""
+    L = ib3d.lib()
+    none = [None] * 7
+    assert L.ib3d_download_fields(None, *none) == ib3d.ERR_ARG
+    assert L.ib3d_download_fields_async(None, *none) == ib3d.ERR_ARG
+    assert L.ib3d_download_wait(None) == ib3d.ERR_ARG
