@@ -108,3 +108,21 @@ def test_download_entry_points_reject_a_null_context(ib3d, built_lib):
     assert L.ib3d_download_fields(None, *none) == ib3d.ERR_ARG
     assert L.ib3d_download_fields_async(None, *none) == ib3d.ERR_ARG
     assert L.ib3d_download_wait(None) == ib3d.ERR_ARG
+
+
+@pytest.mark.parametrize("field,value,accepted", [("sweep_kernel", 4, True), ("sweep_kernel", 5, False),
+                                                  ("sweep_kernel", -1, False), ("precision", 2, True),
+                                                  ("precision", 3, False), ("warm_start", 3, False)])
+def test_create_validates_parameters_before_touching_the_device(ib3d, built_lib, grids, field, value, accepted):
+    """ib3d_create checks its parameters before its first CUDA call: a value out of
+    range is IB3D_ERR_ARG; an accepted one gets as far as the device query, which
+    fails without a GPU (IB3D_ERR_CUDA)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    cs = grids.case("tiny")
+    p = ib3d.default_params()
+    setattr(p, field, value)
+    with pytest.raises(ib3d.IB3DError) as e:
+        ib3d.Solver(cs.x, cs.y, cs.z, p)
+    assert e.value.code == (ib3d.ERR_CUDA if accepted else ib3d.ERR_ARG), (field, value)
